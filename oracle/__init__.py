@@ -1,0 +1,218 @@
+"""CPU oracle for the dense RI contraction path -- TEST INFRASTRUCTURE ONLY.
+
+This package is the checker used by tests/, by ``__graft_entry__.smoke()`` and
+by the CPU-baseline leg of ``bench.py``.  The product library never imports it.
+
+It wraps ``oracle.c`` (a C restatement of ``src/external_libs/restmatr.f90``
+and the composed RI-J/RI-K/exchange contractions over OpenBLAS) and
+``davidson_ref.py`` (a line-by-line restatement of ``src/davidson.rs``).
+All arrays are numpy float64 in column-major (Fortran) order, matching the
+reference's ``MatrixFull``/``RIFull`` storage.
+"""
+from __future__ import annotations
+
+import ctypes
+import glob
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+def openblas_path() -> str:
+    import scipy
+
+    libs = glob.glob(os.path.join(os.path.dirname(scipy.__file__), "..", "scipy.libs", "libscipy_openblas*.so"))
+    if not libs:
+        raise RuntimeError("scipy's bundled OpenBLAS was not found")
+    return os.path.realpath(sorted(libs)[0])
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = ctypes.CDLL(path)
+        rc = L.oracle_init(openblas_path().encode())
+        if rc != 0:
+            raise RuntimeError(f"oracle_init failed ({rc})")
+        L.oracle_exchange_energy.restype = ctypes.c_double
+        L.oracle_get_threads.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def _p(a: np.ndarray):
+    assert a.dtype == np.float64
+    return a.ctypes.data_as(_dp)
+
+
+def _f(a) -> np.ndarray:
+    return np.asfortranarray(np.asarray(a, dtype=np.float64))
+
+
+def set_threads(n: int) -> None:
+    lib().oracle_set_threads(int(n))
+
+
+def get_threads() -> int:
+    return int(lib().oracle_get_threads())
+
+
+# --------------------------------------------------------------------------
+# GEMM seam
+# --------------------------------------------------------------------------
+def general_dgemm_f(a, rng_ra, rng_ca, opa, b, rng_rb, rng_cb, opb, c, rng_rc, rng_cc, alpha, beta):
+    """restmatr.f90:63-107 on column-major numpy matrices; ranges are (start, stop)."""
+    a, b = _f(a), _f(b)
+    assert c.flags.f_contiguous and c.dtype == np.float64
+    L = lib()
+    i = ctypes.c_int
+    L.oracle_general_dgemm_f(
+        _p(a), i(a.shape[0]), i(a.shape[1]), i(rng_ra[0]), i(rng_ra[1] - rng_ra[0]), i(rng_ca[0]),
+        i(rng_ca[1] - rng_ca[0]), ctypes.c_char(opa.encode()),
+        _p(b), i(b.shape[0]), i(b.shape[1]), i(rng_rb[0]), i(rng_rb[1] - rng_rb[0]), i(rng_cb[0]),
+        i(rng_cb[1] - rng_cb[0]), ctypes.c_char(opb.encode()),
+        _p(c), i(c.shape[0]), i(c.shape[1]), i(rng_rc[0]), i(rng_rc[1] - rng_rc[0]), i(rng_cc[0]),
+        i(rng_cc[1] - rng_cc[0]), ctypes.c_double(alpha), ctypes.c_double(beta))
+    return c
+
+
+def dgemm(opa, opb, a, b, alpha=1.0, beta=0.0, c=None):
+    """lapack_dgemm semantics (matrix_blas_lapack.rs:739-774)."""
+    a, b = _f(a), _f(b)
+    m = a.shape[0] if opa == "N" else a.shape[1]
+    k = a.shape[1] if opa == "N" else a.shape[0]
+    n = b.shape[1] if opb == "N" else b.shape[0]
+    if c is None:
+        c = np.zeros((m, n), order="F")
+    lib().oracle_dgemm(ctypes.c_char(opa.encode()), ctypes.c_char(opb.encode()), m, n, k, ctypes.c_double(alpha),
+                       _p(a), max(a.shape[0], 1), _p(b), max(b.shape[0], 1), ctypes.c_double(beta), _p(c), max(m, 1))
+    return c
+
+
+# --------------------------------------------------------------------------
+# RI path
+# --------------------------------------------------------------------------
+def ri_ao2mo(eigenvector, ri3fn, P0=0, P1=None):
+    """ri_ao2mo_f: eigenvector [nb, ns], ri3fn [nb, nb, naux] -> ri3mo [naux, ns, ns]."""
+    C, B = _f(eigenvector), _f(ri3fn)
+    nb, ns = C.shape
+    naux = B.shape[2]
+    P1 = naux if P1 is None else P1
+    out = np.zeros((naux, ns, ns), order="F")
+    lib().oracle_ri_ao2mo_range(_p(C), _p(B), _p(out), ns, nb, naux, int(P0), int(P1))
+    return out
+
+
+def ri_ov_k(C, B, nocc, P0=0, P1=None):
+    """Occupied-virtual block (i,a,P) and RI-K over slabs P0..P1."""
+    C, B = _f(C), _f(B)
+    nb, ns = C.shape
+    naux = B.shape[2]
+    nvir = ns - nocc
+    P1 = naux if P1 is None else P1
+    ov = np.zeros((nocc, nvir, naux), order="F")
+    K = np.zeros((nb, nb), order="F")
+    lib().oracle_ri_ov_k_range(_p(C), _p(B), nb, naux, nocc, nvir, _p(ov), _p(K), int(P0), int(P1))
+    return ov, K
+
+
+def ri_j(B, D):
+    B, D = _f(B), _f(D)
+    nb, naux = B.shape[0], B.shape[2]
+    w = np.zeros(naux)
+    J = np.zeros((nb, nb), order="F")
+    lib().oracle_ri_j(_p(B), _p(D), nb, naux, _p(w), _p(J))
+    return w, J
+
+
+def exchange_energy(D, K) -> float:
+    D, K = _f(D), _f(K)
+    return float(lib().oracle_exchange_energy(_p(D), _p(K), D.shape[0]))
+
+
+def iajb(Bov2d):
+    Bov2d = _f(Bov2d)
+    nov, naux = Bov2d.shape
+    M = np.zeros((nov, nov), order="F")
+    lib().oracle_iajb(_p(Bov2d), nov, naux, _p(M))
+    return M
+
+
+def response_matvec(Bov2d, delta, X):
+    Bov2d, X = _f(Bov2d), _f(X)
+    delta = np.ascontiguousarray(delta, dtype=np.float64)
+    nov, naux = Bov2d.shape
+    nvec = X.shape[1]
+    AX = np.zeros((nov, nvec), order="F")
+    lib().oracle_response_matvec(_p(Bov2d), _p(delta), nov, naux, _p(X), _p(AX), nvec)
+    return AX
+
+
+# --------------------------------------------------------------------------
+# LAPACK seam
+# --------------------------------------------------------------------------
+def dspevx_packed(ap):
+    """lapack_dspevx (matrix_blas_lapack.rs:1075-1095).  Returns (eigvec [n,n], eigval, n_found).
+
+    n is recovered from the packed length through an f32 square root, as the
+    reference does at :1077.
+    """
+    ap = np.array(ap, dtype=np.float64)
+    n = int(np.sqrt(np.float32(8.0 * np.float32(ap.size) + 1.0)) / np.float32(2.0))
+    w = np.zeros(max(n, 1))
+    z = np.zeros((max(n, 1), max(n, 1)), order="F")
+    nf = ctypes.c_int(0)
+    info = lib().oracle_dspevx_packed(n, _p(ap), _p(w), _p(z), ctypes.byref(nf))
+    if info != 0:
+        raise RuntimeError(f"dspevx info={info}")
+    return z[:n, :n], w[:n], nf.value
+
+
+def dsyev(a, jobz="V"):
+    a = np.array(_f(a), order="F")
+    n = a.shape[0]
+    w = np.zeros(n)
+    info = lib().oracle_dsyev(ctypes.c_char(jobz.encode()), n, _p(a), _p(w))
+    if info != 0:
+        raise RuntimeError(f"dsyev info={info}")
+    return (a if jobz == "V" else None), w
+
+
+def full_to_upper_packed(m) -> np.ndarray:
+    """MatrixFull::to_matrixupper: column j keeps rows 0..=j (packed 'U')."""
+    m = _f(m)
+    n = m.shape[0]
+    return np.concatenate([m[: j + 1, j] for j in range(n)]) if n else np.zeros(0)
+
+
+# --------------------------------------------------------------------------
+# Synthetic inputs
+# --------------------------------------------------------------------------
+def synth_ri3ao(seed, nb, naux, P0=0, P1=None):
+    P1 = naux if P1 is None else P1
+    B = np.zeros((nb, nb, P1 - P0), order="F")
+    lib().oracle_synth_ri3ao(ctypes.c_uint64(seed), nb, naux, int(P0), int(P1), _p(B))
+    return B
+
+
+def synth_coef(seed, nb):
+    """C = Q of the Householder QR of an nb x nb N(0,1) matrix (LAPACK dgeqrf/dorgqr via numpy)."""
+    M = np.zeros((nb, nb), order="F")
+    lib().oracle_synth_coef_seed(ctypes.c_uint64(seed), nb, _p(M))
+    Q, _ = np.linalg.qr(M)
+    return np.asfortranarray(Q)
+
+
+def synth_delta(seed, nov):
+    d = np.zeros(nov)
+    lib().oracle_synth_delta(ctypes.c_uint64(seed), ctypes.c_int64(nov), _p(d))
+    return d
+
+
+from .davidson_ref import DavidsonParams, davidson_solve  # noqa: E402,F401
