@@ -1,0 +1,138 @@
+/*
+ * rest_tensors_gb300.h - C ABI of the GB300 (sm_103a) dense RI contraction path.
+ *
+ * Two families of entry points:
+ *
+ *  1. Drop-in replacements for the reference's Fortran seam, with the exact
+ *     Fortran calling convention (every argument by reference, trailing
+ *     underscore, host pointers, column-major storage).  A build that links
+ *     this library instead of librestmatr.so serves the unchanged Rust
+ *     callers (RIFull::ao2mo, _dgemm).
+ *
+ *  2. rt_* functions on device pointers.  They take a cudaStream_t (passed as
+ *     void*), return rt_status, never abort and never trap.  Arrays are
+ *     float64, column-major, in the reference's layouts:
+ *       ri3ao  RIFull [nb, nb, naux]          B[mu + nb*nu + nb*nb*P]       (src/ri.rs:19-40)
+ *       C      MatrixFull [nb, ns]            C[mu + nb*p]                  (src/matrix/mod.rs:473-480)
+ *       ri3mo  RIFull [naux, ns, ns]          R[P + naux*p + naux*ns*q]     (src/ri.rs:382-408)
+ *       ov     [nocc, nvir, naux]             O[i + nocc*a + nocc*nvir*P]
+ *       D,J,K  MatrixFull [nb, nb]
+ *
+ * Precision forms (rt_form):
+ *   RT_FORM_FP64   IEEE float64 throughout (CUDA-core DFMA).
+ *   RT_FORM_SPLIT  each float64 operand split into `nslices` signed 7-bit
+ *                  digits held exactly in BF16, multiplied on the tcgen05
+ *                  tensor cores with exact FP32 accumulation, recombined
+ *                  exactly in 64-bit integers and rounded once to float64.
+ *                  Inputs must be finite; values below 2^-1022 are flushed.
+ *
+ * Calls on one device may come from several host threads; each call is
+ * stream-ordered on the stream it is given.
+ */
+#ifndef REST_TENSORS_GB300_H
+#define REST_TENSORS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int rt_status;
+#define RT_OK 0
+#define RT_ERR_INVALID_ARG 1
+#define RT_ERR_CUDA 2
+#define RT_ERR_NO_MEMORY 3
+#define RT_ERR_UNSUPPORTED 4
+#define RT_ERR_NONFINITE 5
+#define RT_ERR_TIMEOUT 6
+#define RT_ERR_NOT_CONVERGED 7
+
+#define RT_FORM_FP64 0
+#define RT_FORM_SPLIT 1
+
+/* Library version, (major << 16) | minor. */
+int rt_version(void);
+/* Text for a status code. */
+const char* rt_status_string(rt_status s);
+/* Status and message of the most recent failing call on this host thread. */
+rt_status rt_last_status(void);
+const char* rt_last_error(void);
+/* Synchronise `stream` and report device-side findings of kernels launched
+ * since the last check (RT_ERR_NONFINITE for a non-finite input to the split
+ * form, RT_ERR_TIMEOUT for an exhausted bounded wait); clears them. */
+rt_status rt_sync_status(void* stream);
+
+/* ------------------------------------------------------------------------
+ * Drop-in Fortran seam (host pointers).
+ * ------------------------------------------------------------------------ */
+
+/* Replaces ri_ao2mo_f_ (src/external_libs/ffi_restmatr.rs:5-11, implemented at
+ * src/external_libs/restmatr.f90:158-194):
+ *   ri3mo[P,p,q] = sum_{mu,nu} eigenvector[mu,p] ri3fn[mu,nu,P] eigenvector[nu,q]
+ * ri3mo is [num_auxbas, num_states, num_states] (P fastest).  Float64 form.
+ * Failures are reported through rt_last_status()/rt_last_error() (the Fortran
+ * subroutine has no return value) and ri3mo is then left zero-filled. */
+void ri_ao2mo_f_(const double* eigenvector, const double* ri3fn, double* ri3mo, const int* num_states,
+                 const int* num_basis, const int* num_auxbas);
+
+/* Replaces general_dgemm_f_ (src/external_libs/ffi_restmatr.rs:13-24,
+ * restmatr.f90:63-107): on column-major host matrices,
+ *   C[rc, cc] = alpha * op_a(A[ra, ca]) * op_b(B[rb, cb]) + beta * C[rc, cc]
+ * with blocks given by 0-based start and length. */
+void general_dgemm_f_(const double* matr_a, const int* rows_a, const int* columns_a, const int* start_row_a,
+                      const int* len_row_a, const int* start_column_a, const int* len_column_a, const char* opa,
+                      const double* matr_b, const int* rows_b, const int* columns_b, const int* start_row_b,
+                      const int* len_row_b, const int* start_column_b, const int* len_column_b, const char* opb,
+                      double* matr_c, const int* rows_c, const int* columns_c, const int* start_row_c,
+                      const int* len_row_c, const int* start_column_c, const int* len_column_c,
+                      const double* alpha, const double* beta);
+
+/* ------------------------------------------------------------------------
+ * Device-pointer API.
+ * ------------------------------------------------------------------------ */
+
+/* General column-major float64 GEMM on the device, lapack_dgemm semantics
+ * (src/matrix/matrix_blas_lapack.rs:739-774):
+ *   C = alpha * op(A) * op(B) + beta * C,  op in {'N','T'}. */
+rt_status rt_dgemm(char opa, char opb, int m, int n, int k, double alpha, const double* A, int lda, const double* B,
+                   int ldb, double beta, double* C, int ldc, void* stream);
+
+/* Full AO->MO transform, RIFull::ao2mo (src/ri.rs:356-408):
+ *   ri3mo[P,p,q] = (C^T B^P C)[p,q],  C = [nb, ns], B = [nb, nb, naux] symmetric in (mu, nu).
+ * form RT_FORM_FP64 or RT_FORM_SPLIT (nslices 3..8; ignored for FP64). */
+rt_status rt_ri_ao2mo(const double* C, const double* B, double* ri3mo, int nb, int ns, int naux, int form,
+                      int nslices, void* stream);
+
+/* Occupied-virtual transform plus RI-K from one shared half-transform
+ * X^P = B^P C_occ (the first dgemm of restmatr.f90:183-185):
+ *   ov[i,a,P] = (C_occ^T B^P C_vir)[i,a]      (i fastest; C_vir = C + nb*nocc)
+ *   K[mu,nu]  = sum_P (X^P X^P^T)[mu,nu]
+ * C = [nb, nocc + nvir].  Either output pointer may be NULL to skip it. */
+rt_status rt_ri_ov_k(const double* C, const double* B, int nb, int naux, int nocc, int nvir, double* ov, double* K,
+                     int form, int nslices, void* stream);
+
+/* RI-J: w[P] = sum_{mu,nu} B^P[mu,nu] D[mu,nu] ("ip,ip->p", _einsum_02,
+ * src/matrix/matrix_blas_lapack.rs:1293-1310 on the [nb*nb, naux] view of
+ * ri.rs:309-316) and J = sum_P w[P] B^P.  w may be NULL. */
+rt_status rt_ri_j(const double* B, const double* D, int nb, int naux, double* w, double* J, void* stream);
+
+/* Exchange energy E_x = -tr(D K) = -sum_{mu,nu} D[mu,nu] K[mu,nu], reduced in
+ * float64 with a fixed-order tree.  Writes one double to ex_device. */
+rt_status rt_ri_exchange_energy(const double* D, const double* K, int nb, double* ex_device, void* stream);
+
+/* Fill B[nb, nb, naux] with the deterministic synthetic ri3ao tensor of
+ * include/rt_synth.h (slabs P0..P0+nslab-1 of the full tensor, stored from B). */
+rt_status rt_synth_ri3ao(uint64_t seed, int nb, int P0, int nslab, double* B, void* stream);
+
+/* Host-pointer form of rt_ri_ov_k: copies C and B to the device, runs the
+ * path, copies ov and K back, all on the given stream (synchronised on
+ * return).  Host buffers may be pageable or pinned. */
+rt_status rt_ri_ov_k_host(const double* C, const double* B, int nb, int naux, int nocc, int nvir, double* ov,
+                          double* K, int form, int nslices, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* REST_TENSORS_GB300_H */

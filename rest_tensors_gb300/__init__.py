@@ -1,0 +1,323 @@
+"""GB300 (sm_103a) implementation of rest_tensors' dense RI contraction path.
+
+The compute lives in ``librest_tensors_gb300.so`` (CUDA C++, C ABI declared
+in ``include/rest_tensors_gb300.h``).  This module is the host-side mirror of
+the reference's Rust interface for the path, with the same names, argument
+meaning and error behaviour:
+
+* ``RIFull`` / ``MatrixFull``: column-major containers (src/ri.rs:19-40,
+  src/matrix/mod.rs:473-480) with ``RIFull.ao2mo`` (src/ri.rs:356-408) running
+  through the drop-in ``ri_ao2mo_f_`` symbol;
+* ``general_dgemm_f`` and ``_dgemm`` (src/external_libs/mod.rs:60-83,
+  src/matrix/matrix_blas_lapack.rs:122-178) through ``general_dgemm_f_``;
+* device-tensor entry points (``ri_ov_k``, ``ri_ao2mo``, ``ri_j``,
+  ``exchange_energy``, ``dgemm``) taking torch CUDA tensors, for callers that
+  keep data resident in HBM.
+
+There is no CPU fallback: if the native library cannot be loaded, every call
+raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional, Sequence, Tuple
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "librest_tensors_gb300.so")
+
+RT_OK = 0
+RT_FORM_FP64 = 0
+RT_FORM_SPLIT = 1
+DEFAULT_NSLICES = 6
+
+_lib = None
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+class RTError(RuntimeError):
+    """A non-zero rt_status from the native library."""
+
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"rt_status {status}: {msg}")
+        self.status = status
+
+
+def lib() -> ctypes.CDLL:
+    """Load the native library (building it in-tree if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        from . import build as _build
+
+        _build.build()
+    L = ctypes.CDLL(LIB_PATH)
+    c_int, c_dbl, vp = ctypes.c_int, ctypes.c_double, ctypes.c_void_p
+    L.rt_version.restype = c_int
+    L.rt_status_string.restype = ctypes.c_char_p
+    L.rt_status_string.argtypes = [c_int]
+    L.rt_last_error.restype = ctypes.c_char_p
+    L.rt_last_status.restype = c_int
+    L.rt_sync_status.restype = c_int
+    L.rt_sync_status.argtypes = [vp]
+    L.rt_dgemm.restype = c_int
+    L.rt_dgemm.argtypes = [ctypes.c_char, ctypes.c_char, c_int, c_int, c_int, c_dbl, vp, c_int, vp, c_int, c_dbl, vp,
+                           c_int, vp]
+    L.rt_ri_ao2mo.restype = c_int
+    L.rt_ri_ao2mo.argtypes = [vp, vp, vp, c_int, c_int, c_int, c_int, c_int, vp]
+    L.rt_ri_ov_k.restype = c_int
+    L.rt_ri_ov_k.argtypes = [vp, vp, c_int, c_int, c_int, c_int, vp, vp, c_int, c_int, vp]
+    L.rt_ri_ov_k_host.restype = c_int
+    L.rt_ri_ov_k_host.argtypes = [vp, vp, c_int, c_int, c_int, c_int, vp, vp, c_int, c_int, vp]
+    L.rt_ri_j.restype = c_int
+    L.rt_ri_j.argtypes = [vp, vp, c_int, c_int, vp, vp, vp]
+    L.rt_ri_exchange_energy.restype = c_int
+    L.rt_ri_exchange_energy.argtypes = [vp, vp, c_int, vp, vp]
+    L.rt_synth_ri3ao.restype = c_int
+    L.rt_synth_ri3ao.argtypes = [ctypes.c_uint64, c_int, c_int, c_int, vp, vp]
+    L.ri_ao2mo_f_.restype = None
+    L.general_dgemm_f_.restype = None
+    _lib = L
+    return L
+
+
+def _check(status: int) -> None:
+    if status != RT_OK:
+        L = lib()
+        raise RTError(status, L.rt_last_error().decode(errors="replace"))
+
+
+def last_status() -> int:
+    return int(lib().rt_last_status())
+
+
+# --------------------------------------------------------------------------
+# Reference containers
+# --------------------------------------------------------------------------
+class MatrixFull:
+    """Column-major rank-2 tensor (src/matrix/mod.rs:473-480): ``size=[rows, cols]``, ``indicing=[1, rows]``."""
+
+    def __init__(self, size: Sequence[int], data: np.ndarray):
+        self.size = [int(size[0]), int(size[1])]
+        self.indicing = [1, self.size[0]]
+        self.data = np.ascontiguousarray(np.asarray(data, dtype=np.float64).reshape(-1))
+        if self.data.size < self.size[0] * self.size[1]:
+            raise ValueError("MatrixFull::from_vec: vector shorter than the requested shape")
+
+    @classmethod
+    def new(cls, size, value: float = 0.0) -> "MatrixFull":
+        return cls(size, np.full(size[0] * size[1], value, dtype=np.float64))
+
+    @classmethod
+    def from_vec(cls, size, vec) -> "MatrixFull":
+        return cls(size, np.asarray(vec, dtype=np.float64))
+
+    def to_numpy(self) -> np.ndarray:
+        return self.data[: self.size[0] * self.size[1]].reshape(self.size, order="F")
+
+
+class RIFull:
+    """Column-major rank-3 tensor (src/ri.rs:19-40): element [x, y, z] at x + y*X + z*X*Y."""
+
+    def __init__(self, size: Sequence[int], data: np.ndarray):
+        self.size = [int(s) for s in size]
+        self.indicing = [1, self.size[0], self.size[0] * self.size[1]]
+        self.data = np.ascontiguousarray(np.asarray(data, dtype=np.float64).reshape(-1))
+        if self.data.size < int(np.prod(self.size)):
+            raise ValueError("RIFull::from_vec: vector shorter than the requested shape")
+
+    @classmethod
+    def new(cls, size, value: float = 0.0) -> "RIFull":
+        return cls(size, np.full(int(np.prod(size)), value, dtype=np.float64))
+
+    @classmethod
+    def from_vec(cls, size, vec) -> "RIFull":
+        return cls(size, np.asarray(vec, dtype=np.float64))
+
+    def get_reducing_matrix(self, i_reduced: int) -> np.ndarray:
+        """The i-th [x, y] slab (src/ri.rs:92-100), as a column-major view."""
+        n = self.indicing[2]
+        return self.data[n * i_reduced: n * (i_reduced + 1)].reshape(self.size[:2], order="F")
+
+    def to_numpy(self) -> np.ndarray:
+        return self.data[: int(np.prod(self.size))].reshape(self.size, order="F")
+
+    def ao2mo(self, eigenvector: MatrixFull) -> "RIFull":
+        """ao2mo_v02 (src/ri.rs:382-408): [nb, nb, naux] -> [naux, ns, ns] through ri_ao2mo_f_."""
+        nb, ns = eigenvector.size
+        naux = self.size[2]
+        out = RIFull.new([naux, ns, ns], 0.0)
+        ri_ao2mo_f(eigenvector.data, self.data, out.data, ns, nb, naux)
+        return out
+
+
+# --------------------------------------------------------------------------
+# Fortran seam (host pointers)
+# --------------------------------------------------------------------------
+def _hp(a: np.ndarray):
+    if a.dtype != np.float64 or not (a.flags.c_contiguous or a.flags.f_contiguous):
+        raise TypeError("expected a contiguous float64 numpy array")
+    return a.ctypes.data_as(_dp)
+
+
+def ri_ao2mo_f(eigenvector: np.ndarray, ri3fn: np.ndarray, ri3mo: np.ndarray, num_states: int, num_basis: int,
+               num_auxbas: int) -> None:
+    """src/external_libs/mod.rs:6-22 -> ri_ao2mo_f_ (every argument by reference)."""
+    L = lib()
+    i = ctypes.c_int
+    L.ri_ao2mo_f_(_hp(eigenvector), _hp(ri3fn), _hp(ri3mo), ctypes.byref(i(num_states)), ctypes.byref(i(num_basis)),
+                  ctypes.byref(i(num_auxbas)))
+    _check(last_status())
+
+
+def general_dgemm_f(matr_a: np.ndarray, size_a, range_row_a, range_column_a, opa: str,
+                    matr_b: np.ndarray, size_b, range_row_b, range_column_b, opb: str,
+                    matr_c: np.ndarray, size_c, range_row_c, range_column_c, alpha: float, beta: float) -> None:
+    """src/external_libs/mod.rs:60-83: ranges are Python ``range`` objects (start, stop)."""
+    L = lib()
+    i = ctypes.c_int
+    r = ctypes.byref
+
+    def blk(rg):
+        return r(i(rg.start)), r(i(len(rg)))
+
+    ra, la = blk(range_row_a)
+    ca, lca = blk(range_column_a)
+    rb, lb = blk(range_row_b)
+    cb, lcb = blk(range_column_b)
+    rc, lc = blk(range_row_c)
+    cc, lcc = blk(range_column_c)
+    L.general_dgemm_f_(_hp(matr_a), r(i(size_a[0])), r(i(size_a[1])), ra, la, ca, lca, r(ctypes.c_char(opa.encode())),
+                       _hp(matr_b), r(i(size_b[0])), r(i(size_b[1])), rb, lb, cb, lcb, r(ctypes.c_char(opb.encode())),
+                       _hp(matr_c), r(i(size_c[0])), r(i(size_c[1])), rc, lc, cc, lcc,
+                       r(ctypes.c_double(alpha)), r(ctypes.c_double(beta)))
+    _check(last_status())
+
+
+def _dgemm(matr_a: MatrixFull, sub_a: Tuple[range, range], opa: str,
+           matr_b: MatrixFull, sub_b: Tuple[range, range], opb: str,
+           matr_c: MatrixFull, sub_c: Tuple[range, range], alpha: float, beta: float) -> None:
+    """src/matrix/matrix_blas_lapack.rs:122-178, including its shape and bounds checks
+    (the reference panics; this raises ValueError)."""
+    la0, la1 = len(sub_a[0]), len(sub_a[1])
+    lb0, lb1 = len(sub_b[0]), len(sub_b[1])
+    lc0, lc1 = len(sub_c[0]), len(sub_c[1])
+    ok = {
+        ("N", "N"): la1 == lb0 and la0 == lc0 and lb1 == lc1,
+        ("T", "N"): la0 == lb0 and la1 == lc0 and lb1 == lc1,
+        ("N", "T"): la1 == lb1 and la0 == lc0 and lb0 == lc1,
+        ("T", "T"): la0 == lb1 and la1 == lc0 and lb0 == lc1,
+    }.get((opa, opb), False)
+    if not ok:
+        raise ValueError(f"ERROR:: Matr_A[{la0},{la1},{opa}] * Matr_B[{lb0},{lb1},{opb}] -> Matr_C[{lc0},{lc1}]")
+    within = (sub_a[0].stop <= matr_a.size[0] and sub_a[1].stop <= matr_a.size[1]
+              and sub_b[0].stop <= matr_b.size[0] and sub_b[1].stop <= matr_b.size[1]
+              and sub_c[0].stop <= matr_c.size[0] and sub_c[1].stop <= matr_c.size[1])
+    if not within:
+        raise ValueError("ERROR:: sub-matrix block outside the matrix")
+    general_dgemm_f(matr_a.data, matr_a.size, sub_a[0], sub_a[1], opa, matr_b.data, matr_b.size, sub_b[0], sub_b[1],
+                    opb, matr_c.data, matr_c.size, sub_c[0], sub_c[1], alpha, beta)
+
+
+# --------------------------------------------------------------------------
+# Device-tensor API (torch CUDA tensors, float64)
+# --------------------------------------------------------------------------
+def _dptr(t) -> int:
+    import torch
+
+    if t is None:
+        return None
+    if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float64 and t.is_contiguous()):
+        raise TypeError("expected a contiguous float64 CUDA tensor")
+    return t.data_ptr()
+
+
+def _stream(stream) -> int:
+    import torch
+
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return s.cuda_stream
+
+
+def _form(form: str) -> int:
+    if form == "fp64":
+        return RT_FORM_FP64
+    if form == "split":
+        return RT_FORM_SPLIT
+    raise ValueError("form must be 'fp64' or 'split'")
+
+
+def dgemm(opa, opb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, stream=None) -> None:
+    _check(lib().rt_dgemm(opa.encode(), opb.encode(), m, n, k, alpha, _dptr(A), lda, _dptr(B), ldb, beta, _dptr(C),
+                          ldc, _stream(stream)))
+
+
+def ri_ao2mo(C, B, nb: int, ns: int, naux: int, out=None, form: str = "fp64", nslices: int = DEFAULT_NSLICES,
+             stream=None):
+    """Device ri3mo [naux, ns, ns] (P fastest) from device C [nb, ns] and B [nb, nb, naux] (flat tensors)."""
+    import torch
+
+    if out is None:
+        out = torch.empty(naux * ns * ns, dtype=torch.float64, device=C.device)
+    _check(lib().rt_ri_ao2mo(_dptr(C), _dptr(B), _dptr(out), nb, ns, naux, _form(form), nslices, _stream(stream)))
+    return out
+
+
+def ri_ov_k(C, B, nb: int, naux: int, nocc: int, nvir: int, ov=None, K=None, form: str = "split",
+            nslices: int = DEFAULT_NSLICES, stream=None, want_ov: bool = True, want_k: bool = True):
+    """ov (i,a,P) and K [nb, nb] on the device."""
+    import torch
+
+    if want_ov and ov is None:
+        ov = torch.empty(nocc * nvir * naux, dtype=torch.float64, device=C.device)
+    if want_k and K is None:
+        K = torch.empty(nb * nb, dtype=torch.float64, device=C.device)
+    _check(lib().rt_ri_ov_k(_dptr(C), _dptr(B), nb, naux, nocc, nvir, _dptr(ov) if want_ov else None,
+                            _dptr(K) if want_k else None, _form(form), nslices, _stream(stream)))
+    return ov, K
+
+
+def ri_ov_k_host(C: np.ndarray, B: np.ndarray, nb: int, naux: int, nocc: int, nvir: int, ov: np.ndarray,
+                 K: np.ndarray, form: str = "split", nslices: int = DEFAULT_NSLICES, stream=None) -> None:
+    """Host-buffer form (numpy or pinned memory addresses): copies in, runs, copies out."""
+    def hp(a):
+        return a.ctypes.data if isinstance(a, np.ndarray) else int(a)
+
+    _check(lib().rt_ri_ov_k_host(hp(C), hp(B), nb, naux, nocc, nvir, hp(ov), hp(K), _form(form), nslices,
+                                 _stream(stream)))
+
+
+def ri_j(B, D, nb: int, naux: int, w=None, J=None, stream=None):
+    import torch
+
+    if w is None:
+        w = torch.empty(naux, dtype=torch.float64, device=B.device)
+    if J is None:
+        J = torch.empty(nb * nb, dtype=torch.float64, device=B.device)
+    _check(lib().rt_ri_j(_dptr(B), _dptr(D), nb, naux, _dptr(w), _dptr(J), _stream(stream)))
+    return w, J
+
+
+def exchange_energy(D, K, nb: int, out=None, stream=None):
+    import torch
+
+    if out is None:
+        out = torch.empty(1, dtype=torch.float64, device=D.device)
+    _check(lib().rt_ri_exchange_energy(_dptr(D), _dptr(K), nb, _dptr(out), _stream(stream)))
+    return out
+
+
+def synth_ri3ao(seed: int, nb: int, naux: int, P0: int = 0, out=None, stream=None):
+    import torch
+
+    if out is None:
+        out = torch.empty(nb * nb * naux, dtype=torch.float64, device="cuda")
+    _check(lib().rt_synth_ri3ao(seed, nb, P0, naux, _dptr(out), _stream(stream)))
+    return out
+
+
+def sync_status(stream=None) -> None:
+    _check(lib().rt_sync_status(_stream(stream)))

@@ -1,0 +1,293 @@
+// capi.cu - the exported C ABI: the reference's Fortran seam (drop-in, host
+// pointers) and the rt_* device-pointer API, composed from the float64 and
+// split-precision GEMM services.
+#include <string.h>
+
+#include <algorithm>
+
+#include "rt_internal.cuh"
+
+namespace rt {
+
+rt_status ri_j_fp64(const double* B, const double* D, int nb, int naux, double* w, double* J, cudaStream_t stream);
+rt_status exchange_energy(const double* D, const double* K, int nb, double* out, cudaStream_t stream);
+rt_status synth_ri3ao(uint64_t seed, int nb, int P0, int nslab, double* B, cudaStream_t stream);
+rt_status ri_ao2mo_fp64(const double* C, const double* B, double* R, int nb, int ns, int naux, cudaStream_t stream);
+rt_status ri_ov_k_fp64(const double* C, const double* B, int nb, int naux, int nocc, int nvir, double* ov,
+                       double* K, cudaStream_t stream);
+
+namespace {
+
+// Slabs per split-precision block so that the BF16 digit planes of one block
+// stay within ~16 GB of scratch.
+int64_t split_block(int64_t nb, int64_t naux, int S) {
+    const int64_t kpad = (nb + 31) / 32 * 32;
+    const int64_t per = nb * kpad * 2 * S;
+    int64_t blk = ((int64_t)16 << 30) / std::max<int64_t>(per, 1);
+    return std::max<int64_t>(1, std::min<int64_t>(blk, naux));
+}
+
+rt_status ri_ao2mo_split(const double* C, const double* B, double* R, int nb, int ns, int naux, int S,
+                         cudaStream_t stream) {
+    const int64_t blk = split_block(nb, naux, S);
+    const int64_t per = (int64_t)nb * ns;
+    ScratchBuf xb;
+    RT_TRY(scratch_alloc(xb, sizeof(double) * (size_t)(per * blk), stream));
+    double* T = xb.as<double>();
+    for (int64_t P0 = 0; P0 < naux; P0 += blk) {
+        const int64_t np = std::min<int64_t>(blk, naux - P0);
+        // T^P = B^P C: A(m=(mu,P), k=nu) = B[mu + nb nu + nb^2 P], B(n=p, k=nu) = C[nu + nb p]
+        OzGemm g1;
+        g1.K = nb;
+        g1.A.p = B + P0 * (int64_t)nb * nb; g1.A.rows = (int64_t)nb * np; g1.A.div = nb;
+        g1.A.s0 = 1; g1.A.s1 = (int64_t)nb * nb; g1.A.sk = nb;
+        g1.B.p = C; g1.B.rows = ns; g1.B.s0 = nb; g1.B.sk = 1;
+        g1.C.p = T; g1.C.md = nb; g1.C.ms0 = 1; g1.C.ms1 = per; g1.C.ns0 = nb;
+        g1.nslices = S;
+        RT_TRY(oz_gemm(g1, stream));
+        // R^P[p,q] = sum_mu C[mu,p] T^P[mu,q]: A(m=(q,P), k=mu) = T[mu + nb m], B(n=p, k=mu) = C[mu + nb p]
+        OzGemm g2;
+        g2.K = nb;
+        g2.A.p = T; g2.A.rows = (int64_t)ns * np; g2.A.s0 = nb; g2.A.sk = 1;
+        g2.B.p = C; g2.B.rows = ns; g2.B.s0 = nb; g2.B.sk = 1;
+        g2.C.p = R + P0; g2.C.md = ns; g2.C.ms0 = (int64_t)naux * ns; g2.C.ms1 = 1; g2.C.ns0 = naux;
+        g2.nslices = S;
+        RT_TRY(oz_gemm(g2, stream));
+    }
+    return RT_OK;
+}
+
+rt_status ri_ov_k_split(const double* C, const double* B, int nb, int naux, int nocc, int nvir, double* ov,
+                        double* K, int S, cudaStream_t stream) {
+    const int64_t per = (int64_t)nb * nocc;
+    ScratchBuf xb;
+    RT_TRY(scratch_alloc(xb, sizeof(double) * (size_t)(per * naux), stream));
+    double* X = xb.as<double>();
+    const int64_t blk = split_block(nb, naux, S);
+    for (int64_t P0 = 0; P0 < naux; P0 += blk) {
+        const int64_t np = std::min<int64_t>(blk, naux - P0);
+        // X^P = B^P C_occ, stored X[mu + nb i + nb nocc P]
+        OzGemm g1;
+        g1.K = nb;
+        g1.A.p = B + P0 * (int64_t)nb * nb; g1.A.rows = (int64_t)nb * np; g1.A.div = nb;
+        g1.A.s0 = 1; g1.A.s1 = (int64_t)nb * nb; g1.A.sk = nb;
+        g1.B.p = C; g1.B.rows = nocc; g1.B.s0 = nb; g1.B.sk = 1;
+        g1.C.p = X + P0 * per; g1.C.md = nb; g1.C.ms0 = 1; g1.C.ms1 = per; g1.C.ns0 = nb;
+        g1.nslices = S;
+        RT_TRY(oz_gemm(g1, stream));
+        if (ov && nvir > 0) {
+            // ov[i,a,P] = sum_mu X^P[mu,i] C_vir[mu,a]: A(m=(i,P), k=mu) = X[mu + nb m]
+            OzGemm g2;
+            g2.K = nb;
+            g2.A.p = X + P0 * per; g2.A.rows = (int64_t)nocc * np; g2.A.s0 = nb; g2.A.sk = 1;
+            g2.B.p = C + per; g2.B.rows = nvir; g2.B.s0 = nb; g2.B.sk = 1;
+            g2.C.p = ov + P0 * (int64_t)nocc * nvir; g2.C.md = nocc; g2.C.ms0 = 1;
+            g2.C.ms1 = (int64_t)nocc * nvir; g2.C.ns0 = nocc;
+            g2.nslices = S;
+            RT_TRY(oz_gemm(g2, stream));
+        }
+    }
+    if (K) {
+        // K[mu,nu] = sum_{(i,P)} X[mu + nb k] X[nu + nb k], k = i + nocc P
+        OzGemm g3;
+        g3.K = (int64_t)nocc * naux;
+        g3.A.p = X; g3.A.rows = nb; g3.A.s0 = 1; g3.A.sk = nb;
+        g3.B = g3.A;
+        g3.b_is_a = true;
+        g3.symmetric = true;
+        g3.C.p = K; g3.C.ms0 = 1; g3.C.ns0 = nb;
+        g3.nslices = S;
+        RT_TRY(oz_gemm(g3, stream));
+    }
+    return RT_OK;
+}
+
+bool valid_form(int form, int nslices) {
+    return form == RT_FORM_FP64 || (form == RT_FORM_SPLIT && nslices >= 3 && nslices <= 8);
+}
+
+}  // namespace
+}  // namespace rt
+
+using namespace rt;
+
+extern "C" {
+
+rt_status rt_dgemm(char opa, char opb, int m, int n, int k, double alpha, const double* A, int lda, const double* B,
+                   int ldb, double beta, double* C, int ldc, void* stream) {
+    RT_REQUIRE(m >= 0 && n >= 0 && k >= 0, "rt_dgemm: negative dimension");
+    RT_REQUIRE(opa == 'N' || opa == 'T' || opa == 'n' || opa == 't', "rt_dgemm: opa must be N or T");
+    RT_REQUIRE(opb == 'N' || opb == 'T' || opb == 'n' || opb == 't', "rt_dgemm: opb must be N or T");
+    const char oa = (opa == 'n') ? 'N' : (opa == 't' ? 'T' : opa);
+    const char ob = (opb == 'n') ? 'N' : (opb == 't' ? 'T' : opb);
+    RT_REQUIRE(lda >= std::max(1, oa == 'N' ? m : k), "rt_dgemm: lda too small");
+    RT_REQUIRE(ldb >= std::max(1, ob == 'N' ? k : n), "rt_dgemm: ldb too small");
+    RT_REQUIRE(ldc >= std::max(1, m), "rt_dgemm: ldc too small");
+    GemmF64 g;
+    g.opa = oa; g.opb = ob; g.m = m; g.n = n; g.k = k; g.alpha = alpha; g.beta = beta;
+    g.A = A; g.lda = lda; g.B = B; g.ldb = ldb; g.C = C; g.rsC = 1; g.csC = ldc;
+    const int64_t tiles = ceil_div(m, 64) * ceil_div(n, 64);
+    if (tiles < sm_count() && k >= 1024) g.splitk = (int)std::min<int64_t>(ceil_div(2 * sm_count(), tiles), k / 256);
+    return gemm_f64(g, (cudaStream_t)stream);
+}
+
+rt_status rt_ri_ao2mo(const double* C, const double* B, double* ri3mo, int nb, int ns, int naux, int form,
+                      int nslices, void* stream) {
+    RT_REQUIRE(nb >= 0 && ns >= 0 && naux >= 0, "rt_ri_ao2mo: negative dimension");
+    RT_REQUIRE(valid_form(form, nslices), "rt_ri_ao2mo: bad form/nslices (%d, %d)", form, nslices);
+    if ((int64_t)nb * ns * naux == 0) return RT_OK;
+    RT_REQUIRE(C && B && ri3mo, "rt_ri_ao2mo: null pointer");
+    if (form == RT_FORM_FP64) return ri_ao2mo_fp64(C, B, ri3mo, nb, ns, naux, (cudaStream_t)stream);
+    return ri_ao2mo_split(C, B, ri3mo, nb, ns, naux, nslices, (cudaStream_t)stream);
+}
+
+rt_status rt_ri_ov_k(const double* C, const double* B, int nb, int naux, int nocc, int nvir, double* ov, double* K,
+                     int form, int nslices, void* stream) {
+    RT_REQUIRE(nb >= 0 && naux >= 0 && nocc >= 0 && nvir >= 0, "rt_ri_ov_k: negative dimension");
+    RT_REQUIRE(valid_form(form, nslices), "rt_ri_ov_k: bad form/nslices (%d, %d)", form, nslices);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (K && (nocc == 0 || naux == 0) && nb > 0) RT_CUDA_TRY(cudaMemsetAsync(K, 0, sizeof(double) * nb * (size_t)nb, s));
+    if ((int64_t)nb * naux * nocc == 0) {
+        if (ov && nocc * (int64_t)nvir * naux > 0)
+            RT_CUDA_TRY(cudaMemsetAsync(ov, 0, sizeof(double) * (size_t)nocc * nvir * naux, s));
+        return RT_OK;
+    }
+    RT_REQUIRE(C && B, "rt_ri_ov_k: null input pointer");
+    if (form == RT_FORM_FP64) return ri_ov_k_fp64(C, B, nb, naux, nocc, nvir, ov, K, s);
+    return ri_ov_k_split(C, B, nb, naux, nocc, nvir, ov, K, nslices, s);
+}
+
+rt_status rt_ri_j(const double* B, const double* D, int nb, int naux, double* w, double* J, void* stream) {
+    RT_REQUIRE(nb >= 0 && naux >= 0, "rt_ri_j: negative dimension");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (naux == 0) {
+        if (J && nb) RT_CUDA_TRY(cudaMemsetAsync(J, 0, sizeof(double) * nb * (size_t)nb, s));
+        return RT_OK;
+    }
+    if (nb == 0) {
+        if (w) RT_CUDA_TRY(cudaMemsetAsync(w, 0, sizeof(double) * naux, s));
+        return RT_OK;
+    }
+    RT_REQUIRE(B && D, "rt_ri_j: null input pointer");
+    return ri_j_fp64(B, D, nb, naux, w, J, s);
+}
+
+rt_status rt_ri_exchange_energy(const double* D, const double* K, int nb, double* ex_device, void* stream) {
+    RT_REQUIRE(nb >= 0 && ex_device, "rt_ri_exchange_energy: bad argument");
+    return exchange_energy(D, K, nb, ex_device, (cudaStream_t)stream);
+}
+
+rt_status rt_synth_ri3ao(uint64_t seed, int nb, int P0, int nslab, double* B, void* stream) {
+    RT_REQUIRE(nb >= 0 && P0 >= 0 && nslab >= 0, "rt_synth_ri3ao: negative argument");
+    return synth_ri3ao(seed, nb, P0, nslab, B, (cudaStream_t)stream);
+}
+
+rt_status rt_ri_ov_k_host(const double* C, const double* B, int nb, int naux, int nocc, int nvir, double* ov,
+                          double* K, int form, int nslices, void* stream) {
+    RT_REQUIRE(nb >= 0 && naux >= 0 && nocc >= 0 && nvir >= 0, "rt_ri_ov_k_host: negative dimension");
+    RT_REQUIRE(valid_form(form, nslices), "rt_ri_ov_k_host: bad form/nslices");
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t nC = (size_t)nb * (nocc + nvir), nB = (size_t)nb * nb * naux;
+    const size_t nO = (size_t)nocc * nvir * naux, nK = (size_t)nb * nb;
+    ScratchBuf dC, dB, dO, dK;
+    RT_TRY(scratch_alloc(dC, sizeof(double) * std::max<size_t>(nC, 1), s));
+    RT_TRY(scratch_alloc(dB, sizeof(double) * std::max<size_t>(nB, 1), s));
+    if (ov) RT_TRY(scratch_alloc(dO, sizeof(double) * std::max<size_t>(nO, 1), s));
+    if (K) RT_TRY(scratch_alloc(dK, sizeof(double) * std::max<size_t>(nK, 1), s));
+    if (nC) RT_CUDA_TRY(cudaMemcpyAsync(dC.p, C, sizeof(double) * nC, cudaMemcpyHostToDevice, s));
+    if (nB) RT_CUDA_TRY(cudaMemcpyAsync(dB.p, B, sizeof(double) * nB, cudaMemcpyHostToDevice, s));
+    RT_TRY(error_word_reset(s));
+    RT_TRY(rt_ri_ov_k(dC.as<double>(), dB.as<double>(), nb, naux, nocc, nvir, ov ? dO.as<double>() : nullptr,
+                      K ? dK.as<double>() : nullptr, form, nslices, stream));
+    if (ov && nO) RT_CUDA_TRY(cudaMemcpyAsync(ov, dO.p, sizeof(double) * nO, cudaMemcpyDeviceToHost, s));
+    if (K && nK) RT_CUDA_TRY(cudaMemcpyAsync(K, dK.p, sizeof(double) * nK, cudaMemcpyDeviceToHost, s));
+    return error_word_check(s, "rt_ri_ov_k_host");
+}
+
+// ------------------------------------------------------------ Fortran seam --
+
+void ri_ao2mo_f_(const double* eigenvector, const double* ri3fn, double* ri3mo, const int* num_states,
+                 const int* num_basis, const int* num_auxbas) {
+    rt::set_error(RT_OK, "");
+    const int ns = *num_states, nb = *num_basis, naux = *num_auxbas;
+    const size_t nR = (size_t)naux * ns * ns;
+    if (nR) memset(ri3mo, 0, sizeof(double) * nR);
+    if (ns <= 0 || nb <= 0 || naux <= 0) return;
+    cudaStream_t s = cudaStreamPerThread;
+    const size_t nC = (size_t)nb * ns, nB = (size_t)nb * nb * naux;
+    auto run = [&]() -> rt_status {
+        ScratchBuf dC, dB, dR;
+        RT_TRY(scratch_alloc(dC, sizeof(double) * nC, s));
+        RT_TRY(scratch_alloc(dB, sizeof(double) * nB, s));
+        RT_TRY(scratch_alloc(dR, sizeof(double) * nR, s));
+        RT_CUDA_TRY(cudaMemcpyAsync(dC.p, eigenvector, sizeof(double) * nC, cudaMemcpyHostToDevice, s));
+        RT_CUDA_TRY(cudaMemcpyAsync(dB.p, ri3fn, sizeof(double) * nB, cudaMemcpyHostToDevice, s));
+        RT_TRY(rt_ri_ao2mo(dC.as<double>(), dB.as<double>(), dR.as<double>(), nb, ns, naux, RT_FORM_FP64, 0, s));
+        RT_CUDA_TRY(cudaMemcpyAsync(ri3mo, dR.p, sizeof(double) * nR, cudaMemcpyDeviceToHost, s));
+        RT_CUDA_TRY(cudaStreamSynchronize(s));
+        return RT_OK;
+    };
+    if (run() != RT_OK) {
+        memset(ri3mo, 0, sizeof(double) * nR);
+        fprintf(stderr, "ri_ao2mo_f_: %s\n", rt_last_error());
+    }
+}
+
+void general_dgemm_f_(const double* matr_a, const int* rows_a, const int* columns_a, const int* start_row_a,
+                      const int* len_row_a, const int* start_column_a, const int* len_column_a, const char* opa,
+                      const double* matr_b, const int* rows_b, const int* columns_b, const int* start_row_b,
+                      const int* len_row_b, const int* start_column_b, const int* len_column_b, const char* opb,
+                      double* matr_c, const int* rows_c, const int* columns_c, const int* start_row_c,
+                      const int* len_row_c, const int* start_column_c, const int* len_column_c,
+                      const double* alpha, const double* beta) {
+    rt::set_error(RT_OK, "");
+    auto run = [&]() -> rt_status {
+        const char oa = *opa, ob = *opb;
+        RT_REQUIRE(oa == 'N' || oa == 'T', "general_dgemm_f_: opa must be 'N' or 'T'");
+        RT_REQUIRE(ob == 'N' || ob == 'T', "general_dgemm_f_: opb must be 'N' or 'T'");
+        const int m = *len_row_c, n = *len_column_c;
+        const int k = oa == 'N' ? *len_column_a : *len_row_a;
+        const int am = oa == 'N' ? *len_row_a : *len_column_a;
+        const int bk = ob == 'N' ? *len_row_b : *len_column_b;
+        const int bn = ob == 'N' ? *len_column_b : *len_row_b;
+        RT_REQUIRE(am == m && bk == k && bn == n, "general_dgemm_f_: inconsistent block shapes");
+        RT_REQUIRE(*start_row_a >= 0 && *start_row_a + *len_row_a <= *rows_a && *start_column_a >= 0 &&
+                       *start_column_a + *len_column_a <= *columns_a,
+                   "general_dgemm_f_: block of A outside the matrix");
+        RT_REQUIRE(*start_row_b >= 0 && *start_row_b + *len_row_b <= *rows_b && *start_column_b >= 0 &&
+                       *start_column_b + *len_column_b <= *columns_b,
+                   "general_dgemm_f_: block of B outside the matrix");
+        RT_REQUIRE(*start_row_c >= 0 && *start_row_c + m <= *rows_c && *start_column_c >= 0 &&
+                       *start_column_c + n <= *columns_c,
+                   "general_dgemm_f_: block of C outside the matrix");
+        if (m == 0 || n == 0) return RT_OK;
+        cudaStream_t s = cudaStreamPerThread;
+        const int ra = std::max(*len_row_a, 1), rb = std::max(*len_row_b, 1);
+        ScratchBuf dA, dB, dC;
+        RT_TRY(scratch_alloc(dA, sizeof(double) * (size_t)ra * std::max(*len_column_a, 1), s));
+        RT_TRY(scratch_alloc(dB, sizeof(double) * (size_t)rb * std::max(*len_column_b, 1), s));
+        RT_TRY(scratch_alloc(dC, sizeof(double) * (size_t)m * n, s));
+        if (*len_row_a > 0 && *len_column_a > 0)
+            RT_CUDA_TRY(cudaMemcpy2DAsync(dA.p, sizeof(double) * ra,
+                                          matr_a + (size_t)*start_column_a * *rows_a + *start_row_a,
+                                          sizeof(double) * *rows_a, sizeof(double) * *len_row_a, *len_column_a,
+                                          cudaMemcpyHostToDevice, s));
+        if (*len_row_b > 0 && *len_column_b > 0)
+            RT_CUDA_TRY(cudaMemcpy2DAsync(dB.p, sizeof(double) * rb,
+                                          matr_b + (size_t)*start_column_b * *rows_b + *start_row_b,
+                                          sizeof(double) * *rows_b, sizeof(double) * *len_row_b, *len_column_b,
+                                          cudaMemcpyHostToDevice, s));
+        double* cblk = matr_c + (size_t)*start_column_c * *rows_c + *start_row_c;
+        RT_CUDA_TRY(cudaMemcpy2DAsync(dC.p, sizeof(double) * m, cblk, sizeof(double) * *rows_c, sizeof(double) * m,
+                                      n, cudaMemcpyHostToDevice, s));
+        RT_TRY(rt_dgemm(oa, ob, m, n, k, *alpha, dA.as<double>(), ra, dB.as<double>(), rb, *beta, dC.as<double>(),
+                        m, s));
+        RT_CUDA_TRY(cudaMemcpy2DAsync(cblk, sizeof(double) * *rows_c, dC.p, sizeof(double) * m, sizeof(double) * m,
+                                      n, cudaMemcpyDeviceToHost, s));
+        RT_CUDA_TRY(cudaStreamSynchronize(s));
+        return RT_OK;
+    };
+    if (run() != RT_OK) fprintf(stderr, "general_dgemm_f_: %s\n", rt_last_error());
+}
+
+}  // extern "C"

@@ -1,0 +1,404 @@
+// fp64.cu - the plain float64 form of the RI path.
+//
+// GB300 executes float64 on the CUDA cores (DFMA); its tensor cores have no
+// float64 kind and the legacy DMMA path is slower than DFMA on this part
+// (1.05 vs 1.20 TFLOP/s measured).  The plain form is therefore one
+// register-tiled DFMA GEMM service (batched, strided, optional split-K) on
+// which every contraction is composed, plus two DFMA streaming kernels for
+// RI-J and a fixed-order reduction for the exchange energy.
+#include "rt_internal.cuh"
+#include "../../include/rt_synth.h"
+
+namespace rt {
+
+namespace {
+
+constexpr int BM = 64, BN = 64, BK = 16, NT = 256;
+
+struct GemmArgs {
+    int64_t m, n, k;
+    double alpha, beta;
+    const double* A;
+    int64_t lda, sA;
+    const double* B;
+    int64_t ldb, sB;
+    double* C;
+    int64_t rsC, csC, bsC;
+    int64_t batch;
+    int64_t tiles_m, tiles_n;
+    int splitk;
+    int64_t kchunk;
+    double* partial;  // splitk > 1: [splitk][batch][m*n]
+};
+
+// One 64x64 output tile per CTA, 16-deep k slices staged through shared
+// memory, 4x4 outputs per thread.  Thread (tx, ty) owns rows tx + 16*i and
+// columns ty + 16*j, so a warp reads 16 distinct A values and 2 distinct B
+// values per k step (broadcasts, no bank conflicts).
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(NT) dgemm_tile_kernel(GemmArgs g) {
+    __shared__ double As[BK][BM + 1];
+    __shared__ double Bs[BK][BN + 1];
+    const int tid = threadIdx.x;
+    const int tx = tid & 15, ty = tid >> 4;
+    const int64_t tile = blockIdx.x;
+    const int64_t tm = tile % g.tiles_m, tn = tile / g.tiles_m;
+    const int64_t m0 = tm * BM, n0 = tn * BN;
+    const int split = blockIdx.z;
+    const int64_t k0 = (int64_t)split * g.kchunk;
+    const int64_t k1 = min(g.k, k0 + g.kchunk);
+
+    for (int64_t b = blockIdx.y; b < g.batch; b += gridDim.y) {
+        const double* A = g.A + b * g.sA;
+        const double* B = g.B + b * g.sB;
+        double acc[4][4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+
+        for (int64_t kk = k0; kk < k1; kk += BK) {
+            // Stage A tile (BM x BK) as As[k][m].
+#pragma unroll
+            for (int r = 0; r < (BM * BK) / NT; ++r) {
+                int mi, ki;
+                if (!TA) { mi = tid & 63; ki = (tid >> 6) + 4 * r; }
+                else { ki = tid & 15; mi = (tid >> 4) + 16 * r; }
+                const int64_t gm = m0 + mi, gk = kk + ki;
+                double v = 0.0;
+                if (gm < g.m && gk < k1) v = TA ? A[gk + gm * g.lda] : A[gm + gk * g.lda];
+                As[ki][mi] = v;
+            }
+            // Stage B tile (BK x BN) as Bs[k][n].
+#pragma unroll
+            for (int r = 0; r < (BN * BK) / NT; ++r) {
+                int ni, ki;
+                if (!TB) { ki = tid & 15; ni = (tid >> 4) + 16 * r; }
+                else { ni = tid & 63; ki = (tid >> 6) + 4 * r; }
+                const int64_t gn = n0 + ni, gk = kk + ki;
+                double v = 0.0;
+                if (gn < g.n && gk < k1) v = TB ? B[gn + gk * g.ldb] : B[gk + gn * g.ldb];
+                Bs[ki][ni] = v;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int q = 0; q < BK; ++q) {
+                double a[4], bb[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) a[i] = As[q][tx + 16 * i];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) bb[j] = Bs[q][ty + 16 * j];
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], bb[j], acc[i][j]);
+            }
+            __syncthreads();
+        }
+
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int64_t gm = m0 + tx + 16 * i;
+            if (gm >= g.m) continue;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int64_t gn = n0 + ty + 16 * j;
+                if (gn >= g.n) continue;
+                if (g.splitk > 1) {
+                    g.partial[((int64_t)split * g.batch + b) * g.m * g.n + gm + gn * g.m] = acc[i][j];
+                } else {
+                    double* c = g.C + gm * g.rsC + gn * g.csC + b * g.bsC;
+                    double v = g.alpha * acc[i][j];
+                    if (g.beta != 0.0) v = fma(g.beta, *c, v);
+                    *c = v;
+                }
+            }
+        }
+    }
+}
+
+// Deterministic split-K reduction: fixed summation order over the splits.
+__global__ void dgemm_splitk_reduce(GemmArgs g) {
+    const int64_t mn = g.m * g.n;
+    const int64_t total = mn * g.batch;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t b = idx / mn, e = idx % mn;
+        const int64_t i = e % g.m, j = e / g.m;
+        double s = 0.0;
+        for (int z = 0; z < g.splitk; ++z) s += g.partial[((int64_t)z * g.batch + b) * mn + e];
+        double* c = g.C + i * g.rsC + j * g.csC + b * g.bsC;
+        double v = g.alpha * s;
+        if (g.beta != 0.0) v = fma(g.beta, *c, v);
+        *c = v;
+    }
+}
+
+__global__ void scale_kernel(GemmArgs g) {
+    // k == 0: C = beta * C
+    const int64_t mn = g.m * g.n, total = mn * g.batch;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t b = idx / mn, e = idx % mn;
+        double* c = g.C + (e % g.m) * g.rsC + (e / g.m) * g.csC + b * g.bsC;
+        *c = g.beta == 0.0 ? 0.0 : g.beta * *c;
+    }
+}
+
+}  // namespace
+
+rt_status gemm_f64(const GemmF64& q, cudaStream_t stream) {
+    RT_REQUIRE(q.m >= 0 && q.n >= 0 && q.k >= 0 && q.batch >= 0, "gemm_f64: negative size");
+    RT_REQUIRE((q.opa == 'N' || q.opa == 'T') && (q.opb == 'N' || q.opb == 'T'), "gemm_f64: op must be N or T");
+    if (q.m == 0 || q.n == 0 || q.batch == 0) return RT_OK;
+    GemmArgs g{};
+    g.m = q.m; g.n = q.n; g.k = q.k; g.alpha = q.alpha; g.beta = q.beta;
+    g.A = q.A; g.lda = q.lda; g.sA = q.sA; g.B = q.B; g.ldb = q.ldb; g.sB = q.sB;
+    g.C = q.C; g.rsC = q.rsC; g.csC = q.csC; g.bsC = q.bsC; g.batch = q.batch;
+    g.tiles_m = ceil_div(q.m, BM);
+    g.tiles_n = ceil_div(q.n, BN);
+    if (q.k == 0) {
+        scale_kernel<<<1024, 256, 0, stream>>>(g);
+        return check_launch("gemm_f64 scale");
+    }
+    int splitk = q.splitk < 1 ? 1 : q.splitk;
+    int64_t kchunk = ceil_div(ceil_div(q.k, splitk), BK) * BK;
+    splitk = (int)ceil_div(q.k, kchunk);
+    g.splitk = splitk;
+    g.kchunk = kchunk;
+    ScratchBuf part;
+    if (splitk > 1) {
+        RT_TRY(scratch_alloc(part, sizeof(double) * (size_t)splitk * q.batch * q.m * q.n, stream));
+        g.partial = part.as<double>();
+    }
+    dim3 grid((unsigned)(g.tiles_m * g.tiles_n), (unsigned)(q.batch < 65535 ? q.batch : 65535), (unsigned)splitk);
+    const bool ta = q.opa == 'T', tb = q.opb == 'T';
+    if (!ta && !tb) dgemm_tile_kernel<false, false><<<grid, NT, 0, stream>>>(g);
+    else if (ta && !tb) dgemm_tile_kernel<true, false><<<grid, NT, 0, stream>>>(g);
+    else if (!ta && tb) dgemm_tile_kernel<false, true><<<grid, NT, 0, stream>>>(g);
+    else dgemm_tile_kernel<true, true><<<grid, NT, 0, stream>>>(g);
+    RT_TRY(check_launch("dgemm_tile_kernel"));
+    if (splitk > 1) {
+        dgemm_splitk_reduce<<<2 * sm_count(), 256, 0, stream>>>(g);
+        RT_TRY(check_launch("dgemm_splitk_reduce"));
+    }
+    return RT_OK;
+}
+
+// ------------------------------------------------------------------ RI-J --
+
+namespace {
+
+// w[P] = sum_e B[e + n2*P] * D[e]; one CTA per slab, fixed-order block tree.
+__global__ void __launch_bounds__(256) rij_w_kernel(const double* __restrict__ B, const double* __restrict__ D,
+                                                    int64_t n2, int naux, double* __restrict__ w) {
+    __shared__ double red[8];
+    for (int P = blockIdx.x; P < naux; P += gridDim.x) {
+        const double* b = B + (int64_t)P * n2;
+        double s0 = 0.0, s1 = 0.0;
+        int64_t e = threadIdx.x;
+        for (; e + 256 < n2; e += 512) {
+            s0 = fma(b[e], D[e], s0);
+            s1 = fma(b[e + 256], D[e + 256], s1);
+        }
+        if (e < n2) s0 = fma(b[e], D[e], s0);
+        double s = s0 + s1;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            double t = threadIdx.x < 8 ? red[threadIdx.x] : 0.0;
+            for (int o = 4; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+            if (threadIdx.x == 0) w[P] = t;
+        }
+        __syncthreads();
+    }
+}
+
+// J[e] = sum_P w[P] * B[e + n2*P]; each thread owns two adjacent elements and
+// walks the slabs (coalesced 16-byte loads across the warp).
+__global__ void __launch_bounds__(256) rij_j_kernel(const double* __restrict__ B, const double* __restrict__ w,
+                                                    int64_t n2, int naux, double* __restrict__ J) {
+    __shared__ double ws[1024];
+    const int64_t e = 2 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+    double a0 = 0.0, a1 = 0.0, c0 = 0.0, c1 = 0.0;
+    for (int P0 = 0; P0 < naux; P0 += 1024) {
+        const int np = min(1024, naux - P0);
+        __syncthreads();
+        for (int t = threadIdx.x; t < np; t += blockDim.x) ws[t] = w[P0 + t];
+        __syncthreads();
+        if (e + 1 < n2) {
+            const double2* b2 = reinterpret_cast<const double2*>(B + e + (int64_t)P0 * n2);
+            const int64_t st = n2 / 2;
+            int p = 0;
+            for (; p + 1 < np; p += 2) {
+                double2 x = b2[(int64_t)p * st], y = b2[(int64_t)(p + 1) * st];
+                a0 = fma(ws[p], x.x, a0);
+                a1 = fma(ws[p], x.y, a1);
+                c0 = fma(ws[p + 1], y.x, c0);
+                c1 = fma(ws[p + 1], y.y, c1);
+            }
+            if (p < np) {
+                double2 x = b2[(int64_t)p * st];
+                a0 = fma(ws[p], x.x, a0);
+                a1 = fma(ws[p], x.y, a1);
+            }
+        } else if (e < n2) {
+            for (int p = 0; p < np; ++p) a0 = fma(ws[p], B[e + (int64_t)(P0 + p) * n2], a0);
+        }
+    }
+    if (e + 1 < n2) {
+        J[e] = a0 + c0;
+        J[e + 1] = a1 + c1;
+    } else if (e < n2) {
+        J[e] = a0;
+    }
+}
+
+// Same, for odd n2 where 16-byte alignment of every slab cannot be assumed.
+__global__ void __launch_bounds__(256) rij_j_kernel_scalar(const double* __restrict__ B,
+                                                           const double* __restrict__ w, int64_t n2, int naux,
+                                                           double* __restrict__ J) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n2) return;
+    double a0 = 0.0, a1 = 0.0;
+    int p = 0;
+    for (; p + 1 < naux; p += 2) {
+        a0 = fma(w[p], B[e + (int64_t)p * n2], a0);
+        a1 = fma(w[p + 1], B[e + (int64_t)(p + 1) * n2], a1);
+    }
+    if (p < naux) a0 = fma(w[p], B[e + (int64_t)p * n2], a0);
+    J[e] = a0 + a1;
+}
+
+// -tr(D K) with one CTA and a fixed reduction tree (bitwise reproducible).
+__global__ void __launch_bounds__(1024) exchange_kernel(const double* __restrict__ D, const double* __restrict__ K,
+                                                        int64_t n2, double* __restrict__ out) {
+    __shared__ double red[32];
+    double s = 0.0, c = 0.0;  // Kahan-compensated per-thread partial
+    for (int64_t e = threadIdx.x; e < n2; e += blockDim.x) {
+        double y = fma(D[e], K[e], -c);
+        double t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double t = red[threadIdx.x];
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (threadIdx.x == 0) *out = -t;
+    }
+}
+
+__global__ void synth_kernel(uint64_t seed, int nb, int P0, int64_t total, double* B) {
+    const int64_t nb2 = (int64_t)nb * nb;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t P = idx / nb2, r = idx % nb2;
+        const int64_t mu = r % nb, nu = r / nb;
+        B[idx] = rt_ri3ao_elem(seed, P0 + P, mu, nu);
+    }
+}
+
+}  // namespace
+
+rt_status ri_j_fp64(const double* B, const double* D, int nb, int naux, double* w, double* J,
+                    cudaStream_t stream) {
+    const int64_t n2 = (int64_t)nb * nb;
+    ScratchBuf wbuf;
+    if (!w) {
+        RT_TRY(scratch_alloc(wbuf, sizeof(double) * (size_t)naux, stream));
+        w = wbuf.as<double>();
+    }
+    rij_w_kernel<<<(unsigned)naux, 256, 0, stream>>>(B, D, n2, naux, w);
+    RT_TRY(check_launch("rij_w_kernel"));
+    if (J) {
+        if ((n2 & 1) == 0 && ((uintptr_t)B & 15) == 0) {
+            const int64_t threads = n2 / 2;
+            rij_j_kernel<<<(unsigned)ceil_div(threads, 256), 256, 0, stream>>>(B, w, n2, naux, J);
+        } else {
+            rij_j_kernel_scalar<<<(unsigned)ceil_div(n2, 256), 256, 0, stream>>>(B, w, n2, naux, J);
+        }
+        RT_TRY(check_launch("rij_j_kernel"));
+    }
+    return RT_OK;
+}
+
+rt_status exchange_energy(const double* D, const double* K, int nb, double* out, cudaStream_t stream) {
+    exchange_kernel<<<1, 1024, 0, stream>>>(D, K, (int64_t)nb * nb, out);
+    return check_launch("exchange_kernel");
+}
+
+rt_status synth_ri3ao(uint64_t seed, int nb, int P0, int nslab, double* B, cudaStream_t stream) {
+    const int64_t total = (int64_t)nb * nb * nslab;
+    if (total == 0) return RT_OK;
+    synth_kernel<<<8 * sm_count(), 256, 0, stream>>>(seed, nb, P0, total, B);
+    return check_launch("synth_kernel");
+}
+
+// Plain-form AO->MO transform: T^P = B^P C, then R^P = C^T T^P stored P-fastest.
+// Slabs go through in blocks that keep the half-transformed scratch <= ~2 GB.
+rt_status ri_ao2mo_fp64(const double* C, const double* B, double* R, int nb, int ns, int naux,
+                        cudaStream_t stream) {
+    const int64_t per = (int64_t)nb * ns;
+    int64_t blk = (int64_t)((2ull << 30) / (sizeof(double) * (size_t)per));
+    if (blk < 1) blk = 1;
+    if (blk > naux) blk = naux;
+    ScratchBuf tb;
+    RT_TRY(scratch_alloc(tb, sizeof(double) * (size_t)(per * blk), stream));
+    double* T = tb.as<double>();
+    for (int64_t P0 = 0; P0 < naux; P0 += blk) {
+        const int64_t np = std::min<int64_t>(blk, naux - P0);
+        GemmF64 g1;
+        g1.opa = 'N'; g1.opb = 'N'; g1.m = nb; g1.n = ns; g1.k = nb;
+        g1.A = B + P0 * (int64_t)nb * nb; g1.lda = nb; g1.sA = (int64_t)nb * nb;
+        g1.B = C; g1.ldb = nb; g1.sB = 0;
+        g1.C = T; g1.rsC = 1; g1.csC = nb; g1.bsC = per; g1.batch = np;
+        RT_TRY(gemm_f64(g1, stream));
+        GemmF64 g2;
+        g2.opa = 'T'; g2.opb = 'N'; g2.m = ns; g2.n = ns; g2.k = nb;
+        g2.A = C; g2.lda = nb; g2.sA = 0;
+        g2.B = T; g2.ldb = nb; g2.sB = per;
+        g2.C = R + P0; g2.rsC = naux; g2.csC = (int64_t)naux * ns; g2.bsC = 1; g2.batch = np;
+        RT_TRY(gemm_f64(g2, stream));
+    }
+    return RT_OK;
+}
+
+// Plain-form ov transform + RI-K with the shared half-transform X^P = B^P C_occ.
+rt_status ri_ov_k_fp64(const double* C, const double* B, int nb, int naux, int nocc, int nvir, double* ov,
+                       double* K, cudaStream_t stream) {
+    const int64_t per = (int64_t)nb * nocc;
+    ScratchBuf xb;
+    RT_TRY(scratch_alloc(xb, sizeof(double) * (size_t)(per * naux), stream));
+    double* X = xb.as<double>();
+    GemmF64 g1;
+    g1.opa = 'N'; g1.opb = 'N'; g1.m = nb; g1.n = nocc; g1.k = nb;
+    g1.A = B; g1.lda = nb; g1.sA = (int64_t)nb * nb;
+    g1.B = C; g1.ldb = nb; g1.sB = 0;
+    g1.C = X; g1.rsC = 1; g1.csC = nb; g1.bsC = per; g1.batch = naux;
+    RT_TRY(gemm_f64(g1, stream));
+    if (ov && nvir > 0) {
+        GemmF64 g2;
+        g2.opa = 'T'; g2.opb = 'N'; g2.m = nocc; g2.n = nvir; g2.k = nb;
+        g2.A = X; g2.lda = nb; g2.sA = per;
+        g2.B = C + (int64_t)nb * nocc; g2.ldb = nb; g2.sB = 0;
+        g2.C = ov; g2.rsC = 1; g2.csC = nocc; g2.bsC = (int64_t)nocc * nvir; g2.batch = naux;
+        RT_TRY(gemm_f64(g2, stream));
+    }
+    if (K) {
+        GemmF64 g3;
+        g3.opa = 'N'; g3.opb = 'T'; g3.m = nb; g3.n = nb; g3.k = per / nb * naux;
+        g3.A = X; g3.lda = nb; g3.B = X; g3.ldb = nb;
+        g3.C = K; g3.rsC = 1; g3.csC = nb;
+        const int64_t tiles = ceil_div(nb, BM) * ceil_div(nb, BN);
+        const int64_t want = (4 * sm_count() + tiles - 1) / tiles;
+        g3.splitk = (int)std::max<int64_t>(1, std::min<int64_t>(want, g3.k / 256));
+        RT_TRY(gemm_f64(g3, stream));
+    }
+    return RT_OK;
+}
+
+}  // namespace rt

@@ -1,0 +1,641 @@
+// ozaki.cu - split-precision float64 GEMM on the tcgen05 tensor cores.
+//
+// Method (error-free splitting, Ozaki et al., "Error-free transformations of
+// matrix multiplication by using fast routines of matrix multiplication and
+// its applications", Numer. Algorithms 59, 2012; tensor-core variants by
+// Mukunoki et al., ISC 2020):
+//
+//  * Every row of A (and of B, both stored "K-contiguous": C = A B^T) gets a
+//    power-of-two scale from its largest exponent.  Each element is turned,
+//    with integer operations only, into S signed base-128 digits d_0..d_{S-1}
+//    (|d| <= 65, rounded to nearest at the last digit):
+//        x ~= 2^(e_row - 1028) * sum_s d_s 2^(-7 s)
+//    Small integers are exact in BF16, so each digit plane is a BF16 matrix.
+//  * Digit planes are multiplied pairwise on tcgen05 (kind::f16, BF16 in,
+//    FP32 accumulate in tensor memory).  Products of pairs with the same
+//    s + t = g share one TMEM accumulator G_g.  Every partial sum is an
+//    integer below 2^24 in magnitude as long as the contraction is cut into
+//    chunks of at most floor((2^24 - 1) / (S * 65^2)) terms, so the FP32
+//    accumulation is exact.  Pairs with s + t > S - 1 are dropped
+//    (their weight is below the last digit's).
+//  * The epilogue converts each G_g to an integer, forms
+//        V = sum_g G_g 2^(7 (S - 1 - g) - R)
+//    exactly in int64 (R is a right shift that keeps V in range across all
+//    chunks), and rounds once to float64:
+//        C = V * 2^(eA + eB - 2056 - 7 (S - 1) + R).
+//
+// GB300 runs float64 arithmetic at ~1.2 TFLOP/s, so everything above is
+// integer or FP32/BF16 work; the only float64 operations are one int64 ->
+// float64 conversion per output element.
+//
+// Data layout.  Digit planes are written by the slicing kernels directly in
+// the tensor core's shared-memory operand layout (K-major, no swizzle, 8x16B
+// core matrices), pre-tiled as [tile][k-block][digit][T rows x 32 k], so one
+// pipeline stage is a handful of 1-D bulk copies (cp.async.bulk) per operand.
+#include <algorithm>
+
+#include "rt_internal.cuh"
+#include "rt_ptx.cuh"
+
+namespace rt {
+namespace oz {
+
+constexpr int TM = 128;        // rows of A per tile (UMMA M)
+constexpr int TN = 64;         // rows of B per tile (UMMA N)
+constexpr int KB = 32;         // k elements per pipeline stage
+constexpr int NTHREADS = 192;  // warp 0 producer, warp 1 MMA, warps 2..5 epilogue
+constexpr int kSmemBudget = 220 * 1024;
+
+__host__ __device__ constexpr int stage_bytes(int S) { return S * (TM + TN) * KB * 2; }
+__host__ __device__ constexpr int num_stages(int S) {
+    return kSmemBudget / stage_bytes(S) > 6 ? 6 : kSmemBudget / stage_bytes(S);
+}
+// Longest contraction chunk whose group sums stay exact in FP32, in k-blocks.
+__host__ __device__ constexpr int chunk_kblocks(int S) { return (int)(((1 << 24) - 1) / (S * 65 * 65) / KB); }
+__host__ __device__ constexpr int tmem_cols(int S) { return S * TN <= 256 ? 256 : 512; }
+
+// Byte offset of element (r, k) inside one [T x 32] operand block.
+__host__ __device__ __forceinline__ uint32_t core_offset(int r, int k) {
+    return (uint32_t)((r & 7) * 16 + (k & 7) * 2 + (k >> 3) * 128 + (r >> 3) * 512);
+}
+
+struct Operand {
+    const double* p;
+    int64_t rows, div, s0, s1, sk;  // elem(r, k) = p[(r % div) * s0 + (r / div) * s1 + k * sk]
+};
+
+struct SliceArgs {
+    Operand src;
+    int64_t K;
+    int T;          // tile height (128 for A, 64 for B)
+    int64_t tiles;  // ceil(rows / T)
+    int64_t Kb;     // ceil(K / 32)
+    uint16_t* out;  // [tiles][Kb][S][T*32]
+    const int* emax;
+    unsigned int* err;
+};
+
+// ---------------------------------------------------------------- digits --
+
+template <int S>
+struct DigitConst {
+    // q has the row maximum's leading bit at position 61; digit s sits at bit 56 - 7 s.
+    static constexpr unsigned long long rnd = 1ull << (55 - 7 * (S - 1));
+    static constexpr unsigned long long off() {
+        unsigned long long o = 0;
+        for (int k = 1; k < S; ++k) o += 1ull << (62 - 7 * k);
+        return o;
+    }
+};
+
+// Signed base-128 digits of x relative to the row exponent emax (biased).
+template <int S>
+__device__ __forceinline__ void split_digits(double x, int emax, int (&d)[S]) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((bits >> 52) & 0x7FF);
+    const int sh = emax - e + 1;
+    unsigned long long q = 0;
+    if (e != 0 && sh < 64) {
+        const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+        q = (mant << 10) >> sh;
+    }
+    const unsigned long long t = q + (q ? (DigitConst<S>::rnd + DigitConst<S>::off()) : 0ull);
+    const bool neg = (bits >> 63) != 0;
+    if (q == 0) {
+#pragma unroll
+        for (int s = 0; s < S; ++s) d[s] = 0;
+        return;
+    }
+    d[0] = (int)(t >> 56);
+#pragma unroll
+    for (int s = 1; s < S; ++s) d[s] = (int)((t >> (56 - 7 * s)) & 127ull) - 64;
+    if (neg) {
+#pragma unroll
+        for (int s = 0; s < S; ++s) d[s] = -d[s];
+    }
+}
+
+// Exact BF16 bit pattern of a small integer (|v| <= 256).
+__device__ __forceinline__ uint32_t bf16_of_int(int v) {
+    return (uint32_t)__float_as_uint((float)v) >> 16;
+}
+
+// -------------------------------------------------------------- row scale --
+
+// Biased exponent maximum of each row whose k elements are contiguous (sk == 1):
+// one warp per row.
+__global__ void emax_contig_kernel(Operand a, int64_t K, int* __restrict__ emax, unsigned int* err) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r = warp; r < a.rows; r += nwarps) {
+        const double* row = a.p + (r % a.div) * a.s0 + (r / a.div) * a.s1;
+        unsigned int m = 0;
+        for (int64_t k = lane; k < K; k += 32) {
+            const unsigned int e = ((unsigned int)__double2hiint(row[k]) >> 20) & 0x7FFu;
+            m = max(m, e);
+        }
+        m = __reduce_max_sync(0xffffffffu, m);
+        if (lane == 0) {
+            if (m == 0x7FFu) atomicOr(err, DEV_ERR_NONFINITE);
+            emax[r] = (int)m;
+        }
+    }
+}
+
+// Same for rows whose consecutive r are contiguous (s0 == 1): thread per row,
+// blockIdx.y splits k; results combine through atomicMax on a zeroed array.
+__global__ void emax_strided_kernel(Operand a, int64_t K, int64_t kspan, int* __restrict__ emax,
+                                    unsigned int* err) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= a.rows) return;
+    const int64_t k0 = (int64_t)blockIdx.y * kspan, k1 = min(K, k0 + kspan);
+    const double* base = a.p + (r % a.div) * a.s0 + (r / a.div) * a.s1;
+    unsigned int m = 0;
+    for (int64_t k = k0; k < k1; ++k) {
+        const unsigned int e = ((unsigned int)__double2hiint(base[k * a.sk]) >> 20) & 0x7FFu;
+        m = max(m, e);
+    }
+    if (m == 0x7FFu) atomicOr(err, DEV_ERR_NONFINITE);
+    if (m) atomicMax(&emax[r], (int)m);
+}
+
+// --------------------------------------------------------------- slicing --
+
+// Strided rows (s0 == 1): CTA = (tile, k-block); thread handles one row and
+// 32 / (256 / T) consecutive k, reading coalesced across consecutive rows.
+template <int S>
+__global__ void __launch_bounds__(256) slice_strided_kernel(SliceArgs a) {
+    const int T = a.T;
+    const int tpr = 256 / T;    // threads per row
+    const int kper = KB / tpr;  // consecutive k per thread (16 for T=128, 8 for T=64)
+    const int64_t tile = blockIdx.x;
+    const int64_t kb = blockIdx.y;
+    const int r = threadIdx.x % T;
+    const int kq = threadIdx.x / T;
+    const int64_t row = tile * T + r;
+    const bool valid = row < a.src.rows;
+    const int em = valid ? a.emax[row] : 0;
+    const double* base = valid ? a.src.p + (row % a.src.div) * a.src.s0 + (row / a.src.div) * a.src.s1 : nullptr;
+    uint16_t* blk = a.out + ((tile * a.Kb + kb) * S) * (int64_t)(T * KB);
+    for (int g = 0; g < kper; g += 8) {
+        uint32_t w[S][4];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int64_t k = kb * KB + kq * kper + g + j;
+            double x = 0.0;
+            if (valid && k < a.K) x = base[k * a.src.sk];
+            int d[S];
+            split_digits<S>(x, em, d);
+#pragma unroll
+            for (int s = 0; s < S; ++s) {
+                const uint32_t h = bf16_of_int(d[s]);
+                if (j & 1) w[s][j >> 1] |= h << 16;
+                else w[s][j >> 1] = h;
+            }
+        }
+        const int kk = kq * kper + g;
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            uint4 v = make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
+            *reinterpret_cast<uint4*>(reinterpret_cast<uint8_t*>(blk + (int64_t)s * T * KB) + core_offset(r, kk)) = v;
+        }
+    }
+}
+
+// Contiguous rows (sk == 1): CTA = (tile, k-block); the [T x 32] tile is
+// staged through shared memory with coalesced row reads, then sliced as above.
+template <int S>
+__global__ void __launch_bounds__(256) slice_contig_kernel(SliceArgs a) {
+    __shared__ double tileb[TM][KB + 1];
+    const int T = a.T;
+    const int64_t tile = blockIdx.x;
+    const int64_t kb = blockIdx.y;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int rr = wid; rr < T; rr += 8) {
+        const int64_t row = tile * T + rr;
+        const int64_t k = kb * KB + lane;
+        double x = 0.0;
+        if (row < a.src.rows && k < a.K) x = a.src.p[(row % a.src.div) * a.src.s0 + (row / a.src.div) * a.src.s1 + k];
+        tileb[rr][lane] = x;
+    }
+    __syncthreads();
+    const int tpr = 256 / T;
+    const int kper = KB / tpr;
+    const int r = threadIdx.x % T;
+    const int kq = threadIdx.x / T;
+    const int64_t row = tile * T + r;
+    const int em = row < a.src.rows ? a.emax[row] : 0;
+    uint16_t* blk = a.out + ((tile * a.Kb + kb) * S) * (int64_t)(T * KB);
+    for (int g = 0; g < kper; g += 8) {
+        uint32_t w[S][4];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const double x = tileb[r][kq * kper + g + j];
+            int d[S];
+            split_digits<S>(x, em, d);
+#pragma unroll
+            for (int s = 0; s < S; ++s) {
+                const uint32_t h = bf16_of_int(d[s]);
+                if (j & 1) w[s][j >> 1] |= h << 16;
+                else w[s][j >> 1] = h;
+            }
+        }
+        const int kk = kq * kper + g;
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            uint4 v = make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
+            *reinterpret_cast<uint4*>(reinterpret_cast<uint8_t*>(blk + (int64_t)s * T * KB) + core_offset(r, kk)) = v;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ GEMM --
+
+struct OutMap {
+    double* p;
+    int64_t md, ms0, ms1, nd, ns0, ns1;  // addr(m, n) = (m%md)*ms0 + (m/md)*ms1 + (n%nd)*ns0 + (n/nd)*ns1
+};
+
+struct GemmArgs {
+    const uint8_t* a_slices;  // [tiles_m][Kb][S][TM*KB] bf16
+    const uint8_t* b_slices;
+    int64_t b_tile2_stride, b_half_stride, b_kb_stride, b_s_stride;  // bytes; 64-row tile tn -> (tn>>1, tn&1)
+    int64_t a_kb_stride, a_s_stride, a_tile_stride;                  // bytes
+    const int* ea;
+    const int* eb;
+    int64_t M, N, Kb;
+    int64_t tiles_m, tiles_n;
+    int chunk_kb;        // k-blocks per exact chunk
+    int chunks_per_split;
+    int64_t nchunks;     // total chunks
+    int R;               // right shift applied to every group (overflow guard)
+    int symmetric;       // skip tiles strictly below the diagonal
+    OutMap out;
+    int64_t* partial;    // splits > 1: [split][tiles_m*TM][tiles_n*TN]
+    int splits;
+    unsigned int* err;
+};
+
+__device__ __forceinline__ double scale_pow2(int64_t v, int ex) {
+    if (v == 0) return 0.0;
+    double r = __ll2double_rn(v);
+    const int hi = __double2hiint(r), lo = __double2loint(r);
+    const int be = (hi >> 20) & 0x7FF;
+    const int ne = be + ex;
+    if (ne >= 1 && ne <= 2046) return __hiloint2double(hi + (ex << 20), lo);
+    return ldexp(r, ex);
+}
+
+__device__ __forceinline__ int64_t out_addr(const OutMap& o, int64_t m, int64_t n) {
+    return (m % o.md) * o.ms0 + (m / o.md) * o.ms1 + (n % o.nd) * o.ns0 + (n / o.nd) * o.ns1;
+}
+
+template <int S>
+__global__ void __launch_bounds__(NTHREADS, 1) oz_gemm_kernel(GemmArgs a) {
+    constexpr int STAGES = num_stages(S);
+    constexpr uint32_t A_BLK = TM * KB * 2;  // one digit plane, bytes
+    constexpr uint32_t B_BLK = TN * KB * 2;
+    constexpr uint32_t A_STAGE = S * A_BLK;
+    constexpr uint32_t STAGE = S * (A_BLK + B_BLK);
+    constexpr uint32_t NCOLS = tmem_cols(S);
+    constexpr uint32_t IDESC = ptx::idesc_bf16_f32(TM, TN);
+
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE);
+    uint64_t* empty = full + STAGES;
+    uint64_t* acc_full = empty + STAGES;
+    uint64_t* acc_empty = acc_full + 1;
+    uint64_t* drain = acc_empty + 1;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t tn = blockIdx.x % a.tiles_n;
+    const int64_t tm = blockIdx.x / a.tiles_n;
+    const int split = blockIdx.y;
+    if (a.symmetric && (tn * TN + TN - 1) < tm * TM) return;  // strictly below the diagonal
+
+    const int64_t c0 = (int64_t)split * a.chunks_per_split;
+    const int64_t c1 = min(a.nchunks, c0 + a.chunks_per_split);
+    if (c0 >= c1) return;
+    const int64_t kb_begin = c0 * a.chunk_kb;
+    const int64_t kb_end = min(a.Kb, c1 * a.chunk_kb);
+    const int64_t nkb = kb_end - kb_begin;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            ptx::mbar_init(&full[s], 1);
+            ptx::mbar_init(&empty[s], 1);
+        }
+        ptx::mbar_init(acc_full, 1);
+        ptx::mbar_init(acc_empty, 128);
+        ptx::mbar_init(drain, 1);
+        ptx::fence_mbar_init();
+    }
+    if (warp == 1) {
+        ptx::tmem_alloc(tmem_slot, NCOLS);
+        ptx::tmem_relinquish();
+    }
+    ptx::tc_fence_before();
+    __syncthreads();
+    ptx::tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            // ---------------- producer: bulk copies of pre-tiled digit planes
+            int64_t it = 0;
+            bool ok = true;
+            const uint8_t* abase = a.a_slices + tm * a.a_tile_stride;
+            const uint8_t* bbase = a.b_slices + (tn >> 1) * a.b_tile2_stride + (tn & 1) * a.b_half_stride;
+            for (; it < nkb; ++it) {
+                const int st = (int)(it % STAGES);
+                const uint32_t ph = (uint32_t)((it / STAGES) & 1);
+                if (!ptx::mbar_wait(&empty[st], ph ^ 1u, a.err)) { ok = false; break; }
+                uint8_t* sa = smem + st * STAGE;
+                uint8_t* sb = sa + A_STAGE;
+                ptx::mbar_arrive_expect_tx(&full[st], STAGE);
+                const int64_t kb = kb_begin + it;
+                ptx::bulk_g2s(sa, abase + kb * a.a_kb_stride, A_STAGE, &full[st]);
+#pragma unroll
+                for (int s = 0; s < S; ++s)
+                    ptx::bulk_g2s(sb + s * B_BLK, bbase + kb * a.b_kb_stride + s * a.b_s_stride, B_BLK, &full[st]);
+            }
+            if (!ok) {
+                // Let copies already issued land before the CTA can exit.
+                for (int64_t j = max((int64_t)0, it - STAGES); j < it; ++j)
+                    ptx::mbar_wait(&full[j % STAGES], (uint32_t)((j / STAGES) & 1), a.err);
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            // ---------------- MMA issuer
+            bool ok = true;
+            int64_t it = 0;
+            const uint32_t sbase = ptx::smem_u32(smem);
+            for (int64_t c = c0; c < c1 && ok; ++c) {
+                if (c > c0) {
+                    if (!ptx::mbar_wait(acc_empty, (uint32_t)((c - c0 - 1) & 1), a.err)) { ok = false; break; }
+                    ptx::tc_fence_after();
+                }
+                const int64_t cb_end = min(kb_end, (c + 1) * (int64_t)a.chunk_kb);
+                bool first = true;
+                for (int64_t kb = c * a.chunk_kb; kb < cb_end; ++kb, ++it) {
+                    const int st = (int)(it % STAGES);
+                    const uint32_t ph = (uint32_t)((it / STAGES) & 1);
+                    if (!ptx::mbar_wait(&full[st], ph, a.err)) { ok = false; break; }
+                    ptx::tc_fence_after();
+                    const uint32_t sa = sbase + st * STAGE;
+                    const uint32_t sb = sa + A_STAGE;
+#pragma unroll
+                    for (int s = 0; s < S; ++s) {
+#pragma unroll
+                        for (int t = 0; t < S - s; ++t) {
+#pragma unroll
+                            for (int kk = 0; kk < KB / 16; ++kk) {
+                                const uint64_t ad = ptx::smem_desc_kmajor_noswizzle(sa + s * A_BLK + kk * 256, 128, 512);
+                                const uint64_t bd = ptx::smem_desc_kmajor_noswizzle(sb + t * B_BLK + kk * 256, 128, 512);
+                                const uint32_t acc = (first && kk == 0 && s == 0) ? 0u : 1u;
+                                ptx::mma_bf16_ss(tmem + (uint32_t)((s + t) * TN), ad, bd, IDESC, acc);
+                            }
+                        }
+                    }
+                    ptx::mma_commit(&empty[st]);
+                    first = false;
+                }
+                if (ok) ptx::mma_commit(acc_full);
+            }
+            // Every MMA issued so far has completed once `drain` fires.
+            ptx::mma_commit(drain);
+            ptx::mbar_wait(drain, 0, a.err);
+        }
+    } else {
+        // ---------------- epilogue: 4 warps cover the 128 TMEM lanes
+        const int q = warp & 3;
+        const int rl = 32 * q + lane;
+        const int64_t m = tm * TM + rl;
+        int64_t acc[TN];
+#pragma unroll
+        for (int j = 0; j < TN; ++j) acc[j] = 0;
+        bool ok = true;
+        for (int64_t c = c0; c < c1; ++c) {
+            if (!ptx::mbar_wait(acc_full, (uint32_t)((c - c0) & 1), a.err)) { ok = false; break; }
+            ptx::tc_fence_after();
+#pragma unroll
+            for (int g = 0; g < S; ++g) {
+                const int sh = 7 * (S - 1 - g) - a.R;
+#pragma unroll
+                for (int cb = 0; cb < TN / 16; ++cb) {
+                    uint32_t r[16];
+                    ptx::tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(g * TN + cb * 16), r);
+                    ptx::tmem_wait_ld();
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        const int64_t v = (int64_t)__float2int_rn(__uint_as_float(r[j]));
+                        acc[cb * 16 + j] += sh >= 0 ? (v << sh) : ((v + (1ll << (-sh - 1))) >> (-sh));
+                    }
+                }
+            }
+            ptx::tc_fence_before();
+            ptx::mbar_arrive(acc_empty);
+        }
+        if (ok && m < a.M) {
+            if (a.splits > 1) {
+                int64_t* dst = a.partial + ((int64_t)split * a.tiles_m * TM + m) * (a.tiles_n * TN) + tn * TN;
+#pragma unroll
+                for (int j = 0; j < TN; ++j) dst[j] = acc[j];
+            } else {
+                const int ea = a.ea[m];
+                const int base_ex = ea - 2056 - 7 * (S - 1) + a.R;
+#pragma unroll
+                for (int j = 0; j < TN; ++j) {
+                    const int64_t n = tn * TN + j;
+                    if (n < a.N) {
+                        const double v = scale_pow2(acc[j], base_ex + a.eb[n]);
+                        a.out.p[out_addr(a.out, m, n)] = v;
+                    }
+                }
+            }
+        }
+    }
+    ptx::tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        ptx::tc_fence_after();
+        ptx::tmem_dealloc(tmem, NCOLS);
+    }
+}
+
+// Sum split-K int64 partials (exact, order-free) and round once to float64.
+template <int S>
+__global__ void oz_finalize_kernel(GemmArgs a) {
+    const int64_t ldp = a.tiles_n * TN;
+    const int64_t total = a.M * a.N;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t n = idx / a.M, m = idx % a.M;
+        if (a.symmetric && n < m) continue;
+        int64_t v = 0;
+        for (int z = 0; z < a.splits; ++z) v += a.partial[((int64_t)z * a.tiles_m * TM + m) * ldp + n];
+        const int ex = a.ea[m] + a.eb[n] - 2056 - 7 * (S - 1) + a.R;
+        a.out.p[out_addr(a.out, m, n)] = scale_pow2(v, ex);
+    }
+}
+
+// C(m, n) = C(n, m) for m > n (the symmetric product computes n >= m).
+__global__ void mirror_kernel(OutMap o, int64_t N) {
+    const int64_t total = N * N;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t m = idx % N, n = idx / N;
+        if (m > n) o.p[out_addr(o, m, n)] = o.p[out_addr(o, n, m)];
+    }
+}
+
+template <int S>
+void set_smem_attr() {
+    constexpr int bytes = num_stages(S) * stage_bytes(S) + 256;
+    cudaFuncSetAttribute(oz_gemm_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+struct Sliced {
+    ScratchBuf planes, emax;
+    int64_t tiles = 0, Kb = 0;
+    int T = 0;
+};
+
+template <int S>
+rt_status slice_operand(const Operand& op, int64_t K, int T, Sliced& out, cudaStream_t stream) {
+    out.T = T;
+    out.tiles = ceil_div(op.rows, T);
+    out.Kb = ceil_div(K, KB);
+    const size_t plane_bytes = (size_t)out.tiles * T * (size_t)out.Kb * KB * 2 * S;
+    RT_TRY(scratch_alloc(out.planes, plane_bytes, stream));
+    RT_TRY(scratch_alloc(out.emax, sizeof(int) * (size_t)std::max<int64_t>(op.rows, 1), stream));
+    unsigned int* err = error_word_device();
+    RT_REQUIRE(err != nullptr, "oz: device error word unavailable");
+    SliceArgs sa{};
+    sa.src = op; sa.K = K; sa.T = T; sa.tiles = out.tiles; sa.Kb = out.Kb;
+    sa.out = out.planes.as<uint16_t>(); sa.emax = out.emax.as<int>(); sa.err = err;
+    if (op.sk == 1) {
+        const int64_t warps = std::min<int64_t>(op.rows, 64ll * sm_count());
+        emax_contig_kernel<<<(unsigned)ceil_div(warps * 32, 256), 256, 0, stream>>>(op, K, out.emax.as<int>(), err);
+        RT_TRY(check_launch("emax_contig_kernel"));
+        dim3 grid((unsigned)out.tiles, (unsigned)out.Kb);
+        slice_contig_kernel<S><<<grid, 256, 0, stream>>>(sa);
+        RT_TRY(check_launch("slice_contig_kernel"));
+    } else if (op.s0 == 1) {
+        RT_CUDA_TRY(cudaMemsetAsync(out.emax.p, 0, sizeof(int) * (size_t)op.rows, stream));
+        const int64_t kspan = 512;
+        dim3 g1((unsigned)ceil_div(op.rows, 256), (unsigned)ceil_div(K, kspan));
+        emax_strided_kernel<<<g1, 256, 0, stream>>>(op, K, kspan, out.emax.as<int>(), err);
+        RT_TRY(check_launch("emax_strided_kernel"));
+        dim3 grid((unsigned)out.tiles, (unsigned)out.Kb);
+        slice_strided_kernel<S><<<grid, 256, 0, stream>>>(sa);
+        RT_TRY(check_launch("slice_strided_kernel"));
+    } else {
+        set_error(RT_ERR_UNSUPPORTED, "oz: operand needs unit stride along k or along rows");
+        return RT_ERR_UNSUPPORTED;
+    }
+    return RT_OK;
+}
+
+template <int S>
+rt_status run(const OzGemm& g, cudaStream_t stream) {
+    static bool attr_done = false;
+    if (!attr_done) {
+        set_smem_attr<S>();
+        attr_done = true;
+    }
+    Operand A{g.A.p, g.A.rows, g.A.div, g.A.s0, g.A.s1, g.A.sk};
+    Operand B{g.B.p, g.B.rows, g.B.div, g.B.s0, g.B.s1, g.B.sk};
+    Sliced sa, sb;
+    RT_TRY(slice_operand<S>(A, g.K, TM, sa, stream));
+    const bool reuse = g.b_is_a;
+    if (!reuse) RT_TRY(slice_operand<S>(B, g.K, TN, sb, stream));
+
+    GemmArgs a{};
+    a.a_slices = sa.planes.as<uint8_t>();
+    a.a_s_stride = TM * KB * 2;
+    a.a_kb_stride = (int64_t)S * TM * KB * 2;
+    a.a_tile_stride = sa.Kb * a.a_kb_stride;
+    if (reuse) {
+        a.b_slices = sa.planes.as<uint8_t>();
+        a.b_tile2_stride = a.a_tile_stride;
+        a.b_half_stride = TN * KB * 2;
+        a.b_kb_stride = a.a_kb_stride;
+        a.b_s_stride = a.a_s_stride;
+        a.eb = sa.emax.as<int>();
+    } else {
+        a.b_slices = sb.planes.as<uint8_t>();
+        a.b_s_stride = TN * KB * 2;
+        a.b_kb_stride = (int64_t)S * TN * KB * 2;
+        a.b_half_stride = sb.Kb * a.b_kb_stride;
+        a.b_tile2_stride = 2 * a.b_half_stride;
+        a.eb = sb.emax.as<int>();
+    }
+    a.ea = sa.emax.as<int>();
+    a.M = A.rows;
+    a.N = B.rows;
+    a.Kb = sa.Kb;
+    a.tiles_m = ceil_div(a.M, TM);
+    a.tiles_n = ceil_div(a.N, TN);
+    a.chunk_kb = chunk_kblocks(S);
+    a.nchunks = ceil_div(a.Kb, a.chunk_kb);
+    a.symmetric = g.symmetric;
+    a.out = OutMap{g.C.p, g.C.md, g.C.ms0, g.C.ms1, g.C.nd, g.C.ns0, g.C.ns1};
+    a.err = error_word_device();
+
+    // Split the chunk range across CTAs when there are too few tiles to fill the GPU.
+    const int64_t tiles = a.tiles_m * a.tiles_n;
+    int64_t splits = 1;
+    const int64_t want = sm_count();
+    if (tiles < want && a.nchunks > 1) splits = std::min<int64_t>(a.nchunks, ceil_div(want, tiles));
+    a.chunks_per_split = (int)ceil_div(a.nchunks, splits);
+    splits = ceil_div(a.nchunks, a.chunks_per_split);
+    a.splits = (int)splits;
+    // |G_g| < 2^24; V per chunk < 2^(24 + 7(S-1) - R + 0.02); sum over all chunks must stay < 2^62.
+    int lg = 0;
+    while ((1ll << lg) < a.nchunks) ++lg;
+    a.R = std::max(0, 24 + 7 * (S - 1) + 1 + lg - 62);
+
+    ScratchBuf part;
+    if (splits > 1) {
+        RT_TRY(scratch_alloc(part, sizeof(int64_t) * (size_t)splits * a.tiles_m * TM * a.tiles_n * TN, stream));
+        a.partial = part.as<int64_t>();
+    }
+    constexpr int smem = num_stages(S) * stage_bytes(S) + 256;
+    dim3 grid((unsigned)tiles, (unsigned)splits);
+    oz_gemm_kernel<S><<<grid, NTHREADS, smem, stream>>>(a);
+    RT_TRY(check_launch("oz_gemm_kernel"));
+    if (splits > 1) {
+        oz_finalize_kernel<S><<<4 * sm_count(), 256, 0, stream>>>(a);
+        RT_TRY(check_launch("oz_finalize_kernel"));
+    }
+    if (g.symmetric) {
+        mirror_kernel<<<4 * sm_count(), 256, 0, stream>>>(a.out, a.M);
+        RT_TRY(check_launch("mirror_kernel"));
+    }
+    return RT_OK;
+}
+
+}  // namespace oz
+
+rt_status oz_gemm(const OzGemm& g, cudaStream_t stream) {
+    RT_REQUIRE(g.A.rows >= 0 && g.B.rows >= 0 && g.K >= 0, "oz_gemm: negative size");
+    RT_REQUIRE(!g.symmetric || (g.b_is_a && g.A.rows == g.B.rows), "oz_gemm: symmetric needs B == A");
+    if (g.A.rows == 0 || g.B.rows == 0) return RT_OK;
+    switch (g.nslices) {
+        case 3: return oz::run<3>(g, stream);
+        case 4: return oz::run<4>(g, stream);
+        case 5: return oz::run<5>(g, stream);
+        case 6: return oz::run<6>(g, stream);
+        case 7: return oz::run<7>(g, stream);
+        case 8: return oz::run<8>(g, stream);
+        default:
+            set_error(RT_ERR_INVALID_ARG, "nslices must be in 3..8 (got %d)", g.nslices);
+            return RT_ERR_INVALID_ARG;
+    }
+}
+
+}  // namespace rt

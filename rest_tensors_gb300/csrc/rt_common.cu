@@ -1,0 +1,141 @@
+// rt_common.cu - status text, per-thread error messages, the device error
+// word, and stream-ordered scratch allocation.
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <mutex>
+
+#include "rt_internal.cuh"
+
+namespace rt {
+
+static thread_local rt_status g_last_status = RT_OK;
+static thread_local char g_last_msg[512] = "";
+
+void set_error(rt_status s, const char* fmt, ...) {
+    g_last_status = s;
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_last_msg, sizeof(g_last_msg), fmt, ap);
+    va_end(ap);
+}
+
+rt_status last_status() { return g_last_status; }
+
+rt_status check_launch(const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_error(RT_ERR_CUDA, "launch of %s failed: %s", what, cudaGetErrorString(e));
+        return RT_ERR_CUDA;
+    }
+    return RT_OK;
+}
+
+// Device error word: kernels OR flags into it (non-finite input, exhausted
+// bounded waits).  One word per device; it is read and cleared by
+// rt_sync_status() and by the host-pointer entry points.
+__device__ unsigned int g_device_error_word;
+
+unsigned int* error_word_device() {
+    unsigned int* p = nullptr;
+    if (cudaGetSymbolAddress((void**)&p, g_device_error_word) != cudaSuccess) return nullptr;
+    return p;
+}
+
+rt_status error_word_check(cudaStream_t stream, const char* what) {
+    unsigned int* p = error_word_device();
+    if (!p) {
+        set_error(RT_ERR_CUDA, "cannot locate the device error word");
+        return RT_ERR_CUDA;
+    }
+    unsigned int h = 0;
+    RT_CUDA_TRY(cudaMemcpyAsync(&h, p, sizeof(h), cudaMemcpyDeviceToHost, stream));
+    RT_CUDA_TRY(cudaStreamSynchronize(stream));
+    if (h) {
+        RT_CUDA_TRY(cudaMemsetAsync(p, 0, sizeof(unsigned int), stream));
+        RT_CUDA_TRY(cudaStreamSynchronize(stream));
+        if (h & DEV_ERR_TIMEOUT) {
+            set_error(RT_ERR_TIMEOUT, "%s: a device-side wait ran out of its cycle budget", what);
+            return RT_ERR_TIMEOUT;
+        }
+        set_error(RT_ERR_NONFINITE, "%s: the split form received a non-finite input value", what);
+        return RT_ERR_NONFINITE;
+    }
+    return RT_OK;
+}
+
+rt_status error_word_reset(cudaStream_t stream) {
+    unsigned int* p = error_word_device();
+    if (!p) {
+        set_error(RT_ERR_CUDA, "cannot locate the device error word");
+        return RT_ERR_CUDA;
+    }
+    RT_CUDA_TRY(cudaMemsetAsync(p, 0, sizeof(unsigned int), stream));
+    return RT_OK;
+}
+
+int sm_count() {
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 148;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 148;
+    return n;
+}
+
+}  // namespace rt
+
+extern "C" {
+
+int rt_version(void) { return (1 << 16) | 0; }
+
+const char* rt_status_string(rt_status s) {
+    switch (s) {
+        case RT_OK: return "ok";
+        case RT_ERR_INVALID_ARG: return "invalid argument";
+        case RT_ERR_CUDA: return "CUDA error";
+        case RT_ERR_NO_MEMORY: return "out of device memory";
+        case RT_ERR_UNSUPPORTED: return "unsupported configuration";
+        case RT_ERR_NONFINITE: return "non-finite input";
+        case RT_ERR_TIMEOUT: return "device-side wait timed out";
+        case RT_ERR_NOT_CONVERGED: return "not converged";
+        default: return "unknown status";
+    }
+}
+
+rt_status rt_last_status(void) { return rt::g_last_status; }
+const char* rt_last_error(void) { return rt::g_last_msg; }
+
+rt_status rt_sync_status(void* stream) {
+    return rt::error_word_check((cudaStream_t)stream, "device kernels");
+}
+
+}  // extern "C"
+
+namespace rt {
+
+rt_status scratch_alloc(ScratchBuf& b, size_t bytes, cudaStream_t stream) {
+    static std::once_flag once;
+    std::call_once(once, [] {
+        // Keep freed pool memory mapped between calls so repeated calls do
+        // not pay for re-mapping.
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+            uint64_t thr = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+        }
+    });
+    b.s = stream;
+    if (bytes == 0) bytes = 256;
+    cudaError_t e = cudaMallocAsync(&b.p, bytes, stream);
+    if (e != cudaSuccess) {
+        b.p = nullptr;
+        cudaGetLastError();
+        set_error(RT_ERR_NO_MEMORY, "scratch allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+        return RT_ERR_NO_MEMORY;
+    }
+    return RT_OK;
+}
+
+}  // namespace rt

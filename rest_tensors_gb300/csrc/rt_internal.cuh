@@ -1,0 +1,126 @@
+// rt_internal.cuh - shared internals of the GB300 RI-path library.
+//
+// Status/error plumbing, stream-ordered scratch, the device error word, and
+// the two GEMM services (float64 DFMA and split-precision tcgen05).  Everything here is internal; the public C ABI lives in
+// include/rest_tensors_gb300.h.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include "../../include/rest_tensors_gb300.h"
+
+namespace rt {
+
+// Thread-local text of the most recent failure, returned by rt_last_error().
+void set_error(rt_status s, const char* fmt, ...);
+rt_status last_status();
+
+#define RT_CUDA_TRY(expr)                                                                       \
+    do {                                                                                        \
+        cudaError_t _e = (expr);                                                                \
+        if (_e != cudaSuccess) {                                                                \
+            ::rt::set_error(RT_ERR_CUDA, "%s failed: %s (%s:%d)", #expr, cudaGetErrorString(_e), \
+                            __FILE__, __LINE__);                                                \
+            return RT_ERR_CUDA;                                                                 \
+        }                                                                                       \
+    } while (0)
+
+#define RT_TRY(expr)                       \
+    do {                                   \
+        rt_status _s = (expr);             \
+        if (_s != RT_OK) return _s;        \
+    } while (0)
+
+#define RT_REQUIRE(cond, ...)                                  \
+    do {                                                       \
+        if (!(cond)) {                                         \
+            ::rt::set_error(RT_ERR_INVALID_ARG, __VA_ARGS__);  \
+            return RT_ERR_INVALID_ARG;                         \
+        }                                                      \
+    } while (0)
+
+// Check for a launch error right after a <<<>>> launch.
+rt_status check_launch(const char* what);
+
+// Stream-ordered scratch from the device's default memory pool
+// (cudaMallocAsync / cudaFreeAsync on the call's stream), released when the
+// holder goes out of scope.  Concurrent calls on different streams each get
+// their own blocks.
+struct ScratchBuf {
+    void* p = nullptr;
+    cudaStream_t s = nullptr;
+    ScratchBuf() = default;
+    ScratchBuf(const ScratchBuf&) = delete;
+    ScratchBuf& operator=(const ScratchBuf&) = delete;
+    ~ScratchBuf() {
+        if (p) cudaFreeAsync(p, s);
+    }
+    template <typename T>
+    T* as() const { return static_cast<T*>(p); }
+};
+rt_status scratch_alloc(ScratchBuf& b, size_t bytes, cudaStream_t stream);
+
+// Device-wide error word written by kernels that find bad input (non-finite
+// values, exhausted waits); read back by the launching entry point.
+rt_status error_word_reset(cudaStream_t stream);
+rt_status error_word_check(cudaStream_t stream, const char* what);
+unsigned int* error_word_device();
+
+enum : unsigned int {
+    DEV_ERR_NONFINITE = 1u,
+    DEV_ERR_TIMEOUT = 2u,
+};
+
+int sm_count();
+
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// FP64 GEMM service used by every plain-form contraction.  Column-major.
+//   C_b(i,j) = alpha * sum_k opA(A_b)(i,k) opB(B_b)(k,j) + beta * C_b(i,j)
+//   A_b = A + b*sA, B_b = B + b*sB,
+//   C_b(i,j) at C + i*rsC + j*csC + b*bsC   (rsC may differ from 1, e.g. P-fastest outputs)
+struct GemmF64 {
+    char opa = 'N', opb = 'N';
+    int64_t m = 0, n = 0, k = 0;
+    double alpha = 1.0, beta = 0.0;
+    const double* A = nullptr;
+    int64_t lda = 0, sA = 0;
+    const double* B = nullptr;
+    int64_t ldb = 0, sB = 0;
+    double* C = nullptr;
+    int64_t rsC = 1, csC = 0, bsC = 0;
+    int64_t batch = 1;
+    int splitk = 1;  // >1: partial sums in scratch, reduced deterministically
+};
+rt_status gemm_f64(const GemmF64& g, cudaStream_t stream);
+
+// Split-precision (BF16 digit planes on tcgen05, exact integer
+// recombination) GEMM, written as C(m, n) = sum_k A(m, k) * B(n, k):
+//   A(m, k) at A.p[(m % A.div) * A.s0 + (m / A.div) * A.s1 + k * A.sk]   (likewise B)
+//   C(m, n) at C.p[(m % md) * ms0 + (m / md) * ms1 + (n % nd) * ns0 + (n / nd) * ns1]
+// Each operand needs unit stride along k (sk == 1) or along rows (s0 == 1).
+// nslices in [3, 8].  b_is_a reuses A's digit planes for B; symmetric (with
+// b_is_a) computes only n >= m and mirrors.
+constexpr int64_t kNoDiv = (int64_t)1 << 62;
+struct OzOperand {
+    const double* p = nullptr;
+    int64_t rows = 0, div = kNoDiv, s0 = 0, s1 = 0, sk = 1;
+};
+struct OzOut {
+    double* p = nullptr;
+    int64_t md = kNoDiv, ms0 = 1, ms1 = 0, nd = kNoDiv, ns0 = 0, ns1 = 0;
+};
+struct OzGemm {
+    int64_t K = 0;
+    OzOperand A, B;
+    OzOut C;
+    int nslices = 6;
+    bool b_is_a = false;
+    bool symmetric = false;
+};
+rt_status oz_gemm(const OzGemm& g, cudaStream_t stream);
+
+}  // namespace rt
