@@ -1,0 +1,354 @@
+#!/usr/bin/env python
+"""Throughput of the RI occupied-virtual transform + RI-K on GB300.
+
+Workload (one step): nbas=600, naux=2400, nocc=60, nvir=540.  ri3ao B
+[600, 600, 2400] float64 (6.9 GB, larger than L2) from the seeded synthetic
+generator, C = Q of the QR factorisation of a seeded N(0,1) 600x600 matrix.
+A step produces ov[i,a,P] (622 MB) and K[mu,nu] from the shared
+half-transform X^P = B^P C_occ.  Algorithmic work per step (float64
+equivalent, no symmetry credit): naux*(4*nb^2*nocc + 2*nb*nocc*nvir) =
+3.007e11 FLOP.
+
+`value` is the split-precision form (BF16 digit planes on tcgen05) with
+inputs resident in HBM; the float64 form, the split form's error against it,
+the end-to-end number through the host-pointer C ABI, the dominant kernel's
+roofline and the CPU baseline are reported beside it on the same JSON line.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "RI transform+RI-K TFLOP/s: split-prec vs FP64 on one GB300 at err≤1e-10"
+NB, NAUX, NOCC = 600, 2400, 60
+NVIR = NB - NOCC
+FLOPS_PER_SLAB = 4 * NB * NB * NOCC + 2 * NB * NOCC * NVIR
+FLOPS = NAUX * FLOPS_PER_SLAB  # 3.007e11
+
+
+FALLBACK_PEAKS = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}
+
+
+def workload():
+    return f"ri_ov_transform_plus_rik nbas={NB} naux={NAUX} nocc={NOCC} nvir={NVIR}"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=100)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--nslices", type=int, default=7)
+    p.add_argument("--seed", type=int, default=0)
+    p.add_argument("--fp64-steps", type=int, default=2)
+    p.add_argument("--e2e-steps", type=int, default=5)
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--sweep", default="", help="comma list of slice counts to also report (time, errors)")
+    p.add_argument("--naux", type=int, default=NAUX, help="auxiliary slabs (smaller values only for profiling runs)")
+    return p.parse_args()
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(path))
+        return d, "measured"
+    except Exception:
+        return dict(FALLBACK_PEAKS), "fallback"
+
+
+# ----------------------------------------------------------------- clocks --
+class ClockSampler:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200", "-i", str(gpu_index)], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.flush()
+        rows = []
+        for line in open(self.f.name):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.f.name)
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i in range(4) if r[i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ------------------------------------------------------------ CPU baseline --
+def cpu_baseline(seed: int, budget_s: float = 12.0):
+    """Oracle (C restatement of restmatr.f90 + OpenBLAS, all host threads) on a bounded slab range."""
+    import numpy as np
+
+    import oracle
+
+    cores = os.cpu_count() or 1
+    oracle.set_threads(cores)
+    C = oracle.synth_coef(seed, NB)
+    probe = 24
+    B = oracle.synth_ri3ao(seed, NB, NAUX, 0, probe)
+    oracle.ri_ov_k(C, B, NOCC)  # warm-up (threads, pages)
+    t0 = time.perf_counter()
+    oracle.ri_ov_k(C, B, NOCC)
+    per_slab = (time.perf_counter() - t0) / probe
+    nslab = int(max(probe, min(NAUX, budget_s / max(per_slab, 1e-9))))
+    B = oracle.synth_ri3ao(seed, NB, NAUX, 0, nslab)
+    t0 = time.perf_counter()
+    oracle.ri_ov_k(C, B, NOCC)
+    dt = time.perf_counter() - t0
+    del B
+    np.asarray(0)
+    return {"value": nslab * FLOPS_PER_SLAB / dt / 1e12, "unit": "TFLOP/s", "cores": oracle.get_threads(),
+            "kind": "port",
+            "sample": f"{nslab} of {NAUX} aux slabs of the same workload ({dt:.1f} s), C restatement of "
+                      f"restmatr.f90 per-slab dgemms over OpenBLAS (scipy bundle)",
+            "seconds": dt}
+
+
+def run_reference(args, rank: int):
+    global NAUX, FLOPS
+    NAUX = args.naux
+    FLOPS = NAUX * FLOPS_PER_SLAB
+    if rank != 0:
+        return
+    per_step_budget = max(1.0, min(20.0, 150.0 / max(1, args.steps + args.warmup)))
+    import oracle
+
+    cores = os.cpu_count() or 1
+    oracle.set_threads(cores)
+    C = oracle.synth_coef(args.seed, NB)
+    probe = 24
+    B = oracle.synth_ri3ao(args.seed, NB, NAUX, 0, probe)
+    oracle.ri_ov_k(C, B, NOCC)
+    t0 = time.perf_counter()
+    oracle.ri_ov_k(C, B, NOCC)
+    per_slab = (time.perf_counter() - t0) / probe
+    nslab = int(max(probe, min(NAUX, per_step_budget / max(per_slab, 1e-9))))
+    B = oracle.synth_ri3ao(args.seed, NB, NAUX, 0, nslab)
+    for _ in range(args.warmup):
+        oracle.ri_ov_k(C, B, NOCC)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.ri_ov_k(C, B, NOCC)
+    dt = (time.perf_counter() - t0) / max(1, args.steps)
+    v = nslab * FLOPS_PER_SLAB / dt / 1e12
+    sample = (f"each step: {nslab} of {NAUX} aux slabs of the same workload, C restatement of restmatr.f90 "
+              f"per-slab dgemms over OpenBLAS (the reference's own path cannot be built: Rust+Fortran "
+              f"toolchains absent)")
+    line = {"metric": METRIC, "value": v, "unit": "TFLOP/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": workload(), "nbas": NB, "naux": NAUX, "nocc": NOCC, "nvir": NVIR,
+                       "parallelism": "host threads"},
+            "cpu_baseline": {"value": v, "unit": "TFLOP/s", "cores": oracle.get_threads(), "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": v, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# -------------------------------------------------------------------- ours --
+def main():
+    global NAUX, FLOPS
+    args = parse()
+    NAUX = args.naux
+    FLOPS = NAUX * FLOPS_PER_SLAB
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+    assert args.warmup >= 3, "at least 3 warm-up steps"
+    import torch
+
+    import rest_tensors_gb300 as rt
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    S = args.nslices
+
+    B = rt.synth_ri3ao(args.seed, NB, NAUX)
+    C = rt.synth_coef(args.seed, NB)
+    Cm = C.view(NB, NB).t()  # Cm[mu, p] (column-major storage)
+    D = (Cm[:, :NOCC] @ Cm[:, :NOCC].t()).t().contiguous().view(-1)
+    ov = torch.empty(NOCC * NVIR * NAUX, dtype=torch.float64, device=dev)
+    K = torch.empty(NB * NB, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def step(form, nsl):
+        rt.ri_ov_k(C, B, NB, NAUX, NOCC, NVIR, ov=ov, K=K, form=form, nslices=nsl, stream=stream)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    def timed(form, nsl, steps, prof=False):
+        barrier()
+        n0 = rt.launch_count()
+        if prof:
+            rt.profile_enable(True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            step(form, nsl)
+        e1.record(stream)
+        barrier()
+        ms = e0.elapsed_time(e1) / steps
+        launches = rt.launch_count() - n0
+        if dist is not None:
+            t = torch.tensor([ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, launches
+
+    # ---- float64 reference result and its timing
+    step("fp64", 0)
+    rt.sync_status()
+    ov64, K64 = ov.clone(), K.clone()
+    ex64 = rt.exchange_energy(D, K64, NB).item()
+    fp64_ms, _ = timed("fp64", 0, args.fp64_steps)
+    # Accurate E_x reference: the occupied-occupied block B_ij^P = (C_occ^T B^P C_occ)_ij
+    # in float64 (600-term dot products per element), then -sum of squares with a tree sum.
+    Coo = torch.cat([C[: NB * NOCC], C[: NB * NOCC]])
+    oo, _ = rt.ri_ov_k(Coo, B, NB, NAUX, NOCC, NOCC, form="fp64", want_k=False, stream=stream)
+    ex_ref = -float((oo * oo).sum())
+    del oo
+
+    def errors():
+        ex = rt.exchange_energy(D, K, NB).item()
+        return {"ov_max_abs": float((ov - ov64).abs().max()),
+                "K_max_rel": float((K - K64).abs().max() / K64.abs().max()),
+                "ex_abs": abs(ex - ex64), "ex_rel": abs(ex - ex64) / abs(ex64), "ex_fp64": ex64,
+                "ex_abs_vs_oo_ref": abs(ex - ex_ref), "ex_fp64_abs_vs_oo_ref": abs(ex64 - ex_ref),
+                "ex_oo_ref": ex_ref}
+
+    sweep = {}
+    for s in [int(x) for x in args.sweep.split(",") if x.strip()]:
+        for _ in range(2):
+            step("split", s)
+        ms_s, _ = timed("split", s, max(3, args.steps // 5))
+        sweep[str(s)] = {"ms_per_step": ms_s, "tflops": FLOPS / ms_s / 1e9, **errors()}
+
+    # ---- split form: warm-up, then the timed region (clocks sampled meanwhile)
+    for _ in range(args.warmup):
+        step("split", S)
+    rt.sync_status()
+    err = errors()
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+    gpu_index = int(vis.split(",")[local]) if vis and vis.split(",")[local].strip().isdigit() else local
+    sampler = ClockSampler(gpu_index) if rank == 0 else None
+    ms, launches = timed("split", S, args.steps, prof=True)
+    clocks = sampler.stop() if sampler else None
+    g_ms, g_n, g_flops = rt.profile_get(rt.PROF_OZ_GEMM)
+    s_ms, s_n, s_bytes = rt.profile_get(rt.PROF_OZ_SLICE)
+    rt.profile_enable(False)
+    rt.sync_status()
+
+    value = world * FLOPS / ms / 1e9  # TFLOP/s over all ranks
+    pk, pk_kind = peaks()
+    achieved = g_flops / g_ms / 1e9 if g_ms > 0 else None
+    peak = pk.get("bf16_tflops_sustained", FALLBACK_PEAKS["bf16_tflops_sustained"])
+    roofline = {"kernel": "oz_gemm_kernel (tcgen05 BF16 digit-pair GEMM)", "bound": "tensor",
+                "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": (achieved / peak) if achieved else None, "traffic": None,
+                "peak_source": f"{pk_kind} bf16_tflops_sustained (kernel timed inside a continuous step loop)",
+                "launches_per_step": g_n / args.steps, "share_of_step": g_ms / (ms * args.steps),
+                "slicing": {"kernel": "emax/slice kernels (HBM)", "achieved_gbs": s_bytes / s_ms / 1e6 if s_ms else None,
+                            "peak_gbs": pk.get("hbm_gbs"), "share_of_step": s_ms / (ms * args.steps)}}
+
+    # ---- end to end through the host-pointer C ABI (pinned host buffers)
+    e2e = None
+    if args.e2e_steps > 0:
+        hB = torch.empty(NB * NB * NAUX, dtype=torch.float64, pin_memory=True)
+        hB.copy_(B)
+        hC = torch.empty(NB * NB, dtype=torch.float64, pin_memory=True)
+        hC.copy_(C)
+        hO = torch.empty(NOCC * NVIR * NAUX, dtype=torch.float64, pin_memory=True)
+        hK = torch.empty(NB * NB, dtype=torch.float64, pin_memory=True)
+        rt.ri_ov_k_host(hC.data_ptr(), hB.data_ptr(), NB, NAUX, NOCC, NVIR, hO.data_ptr(), hK.data_ptr(),
+                        form="split", nslices=S, stream=stream)
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            rt.ri_ov_k_host(hC.data_ptr(), hB.data_ptr(), NB, NAUX, NOCC, NVIR, hO.data_ptr(), hK.data_ptr(),
+                            form="split", nslices=S, stream=stream)
+        e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+        if dist is not None:
+            t = torch.tensor([e2e_s], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        e2e = {"value": world * FLOPS / e2e_s / 1e12, "unit": "TFLOP/s", "ms_per_step": e2e_s * 1e3,
+               "h2d_bytes_per_step": 8 * (NB * NB * NAUX + NB * NB), "d2h_bytes_per_step": 8 * (NOCC * NVIR * NAUX + NB * NB),
+               "path": "rt_ri_ov_k_host (C ABI, pinned host buffers, copies inside the timed region)"}
+        del hB
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(args.seed)
+
+    if rank != 0:
+        return
+    line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": workload(), "nbas": NB, "naux": NAUX, "nocc": NOCC, "nvir": NVIR,
+                       "form": f"split: {S} BF16 digits per float64, exact FP32 accumulate, int64 recombination",
+                       "nslices": S, "l2": "inputs larger than L2 (6.9 GB ri3ao read per step)",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "fp64": {"value": world * FLOPS / fp64_ms / 1e9, "unit": "TFLOP/s", "ms_per_step": fp64_ms,
+                     "form": "float64 DFMA tiled GEMM"},
+            "speedup_vs_fp64": fp64_ms / ms,
+            "errors_vs_fp64": err, "gpu_launches": launches, "clocks": clocks, "roofline": roofline,
+            "e2e": e2e, "cpu_baseline": cpu}
+    if sweep:
+        line["sweep"] = sweep
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

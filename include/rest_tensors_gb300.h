@@ -98,6 +98,15 @@ void general_dgemm_f_(const double* matr_a, const int* rows_a, const int* column
 rt_status rt_dgemm(char opa, char opb, int m, int n, int k, double alpha, const double* A, int lda, const double* B,
                    int ldb, double beta, double* C, int ldc, void* stream);
 
+/* The same product in the split-precision form: C = op(A) * op(B) (alpha = 1,
+ * beta = 0), each float64 operand cut into `nslices` BF16 digit planes per row
+ * of op(A) and column of op(B), multiplied on the tcgen05 tensor cores and
+ * recombined exactly.  Inputs must be finite.  A call with B == A, ldb == lda,
+ * m == n and opposite ops (A A^T or A^T A) is computed as a symmetric rank-k
+ * update: one set of digit planes, one triangle, mirrored. */
+rt_status rt_dgemm_split(char opa, char opb, int m, int n, int k, const double* A, int lda, const double* B, int ldb,
+                         double* C, int ldc, int nslices, void* stream);
+
 /* Full AO->MO transform, RIFull::ao2mo (src/ri.rs:356-408):
  *   ri3mo[P,p,q] = (C^T B^P C)[p,q],  C = [nb, ns], B = [nb, nb, naux] symmetric in (mu, nu).
  * form RT_FORM_FP64 or RT_FORM_SPLIT (nslices 3..8; ignored for FP64). */
@@ -125,11 +134,30 @@ rt_status rt_ri_exchange_energy(const double* D, const double* K, int nb, double
  * include/rt_synth.h (slabs P0..P0+nslab-1 of the full tensor, stored from B). */
 rt_status rt_synth_ri3ao(uint64_t seed, int nb, int P0, int nslab, double* B, void* stream);
 
+/* Fill M[nb, nb] with the N(0,1) matrix whose QR factor gives the synthetic
+ * orbital coefficients (include/rt_synth.h, rt_coef_seed_elem). */
+rt_status rt_synth_coef_seed(uint64_t seed, int nb, double* M, void* stream);
+
 /* Host-pointer form of rt_ri_ov_k: copies C and B to the device, runs the
  * path, copies ov and K back, all on the given stream (synchronised on
  * return).  Host buffers may be pageable or pinned. */
 rt_status rt_ri_ov_k_host(const double* C, const double* B, int nb, int naux, int nocc, int nvir, double* ov,
                           double* K, int form, int nslices, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Instrumentation.
+ * ------------------------------------------------------------------------ */
+
+/* Number of kernels this library has launched in the process so far. */
+long long rt_launch_count(void);
+/* Enable (1) or disable (0) per-kernel CUDA-event timing; either call clears
+ * the records.  Kinds: 0 split-precision GEMM (flops = BF16 digit-pair
+ * tensor operations), 1 digit slicing (bytes), 2 float64 GEMM (flops),
+ * 3 RI-J streaming (bytes). */
+void rt_profile_enable(int on);
+/* Total event time, launch count and algorithmic work recorded for a kind
+ * (synchronises the recorded events). */
+rt_status rt_profile_get(int kind, double* total_ms, long long* launches, double* work);
 
 #ifdef __cplusplus
 }

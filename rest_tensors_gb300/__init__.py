@@ -66,6 +66,9 @@ def lib() -> ctypes.CDLL:
     L.rt_dgemm.restype = c_int
     L.rt_dgemm.argtypes = [ctypes.c_char, ctypes.c_char, c_int, c_int, c_int, c_dbl, vp, c_int, vp, c_int, c_dbl, vp,
                            c_int, vp]
+    L.rt_dgemm_split.restype = c_int
+    L.rt_dgemm_split.argtypes = [ctypes.c_char, ctypes.c_char, c_int, c_int, c_int, vp, c_int, vp, c_int, vp, c_int,
+                                 c_int, vp]
     L.rt_ri_ao2mo.restype = c_int
     L.rt_ri_ao2mo.argtypes = [vp, vp, vp, c_int, c_int, c_int, c_int, c_int, vp]
     L.rt_ri_ov_k.restype = c_int
@@ -78,6 +81,14 @@ def lib() -> ctypes.CDLL:
     L.rt_ri_exchange_energy.argtypes = [vp, vp, c_int, vp, vp]
     L.rt_synth_ri3ao.restype = c_int
     L.rt_synth_ri3ao.argtypes = [ctypes.c_uint64, c_int, c_int, c_int, vp, vp]
+    L.rt_synth_coef_seed.restype = c_int
+    L.rt_synth_coef_seed.argtypes = [ctypes.c_uint64, c_int, vp, vp]
+    L.rt_launch_count.restype = ctypes.c_longlong
+    L.rt_profile_enable.restype = None
+    L.rt_profile_enable.argtypes = [c_int]
+    L.rt_profile_get.restype = c_int
+    L.rt_profile_get.argtypes = [c_int, ctypes.POINTER(c_dbl), ctypes.POINTER(ctypes.c_longlong),
+                                 ctypes.POINTER(c_dbl)]
     L.ri_ao2mo_f_.restype = None
     L.general_dgemm_f_.restype = None
     _lib = L
@@ -255,6 +266,12 @@ def dgemm(opa, opb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, stream=None) -
                           ldc, _stream(stream)))
 
 
+def dgemm_split(opa, opb, m, n, k, A, lda, B, ldb, C, ldc, nslices: int = DEFAULT_NSLICES, stream=None) -> None:
+    """C = op(A) op(B) in the split-precision form (float64 in and out)."""
+    _check(lib().rt_dgemm_split(opa.encode(), opb.encode(), m, n, k, _dptr(A), lda, _dptr(B), ldb, _dptr(C), ldc,
+                                nslices, _stream(stream)))
+
+
 def ri_ao2mo(C, B, nb: int, ns: int, naux: int, out=None, form: str = "fp64", nslices: int = DEFAULT_NSLICES,
              stream=None):
     """Device ri3mo [naux, ns, ns] (P fastest) from device C [nb, ns] and B [nb, nb, naux] (flat tensors)."""
@@ -317,6 +334,39 @@ def synth_ri3ao(seed: int, nb: int, naux: int, P0: int = 0, out=None, stream=Non
         out = torch.empty(nb * nb * naux, dtype=torch.float64, device="cuda")
     _check(lib().rt_synth_ri3ao(seed, nb, P0, naux, _dptr(out), _stream(stream)))
     return out
+
+
+def synth_coef(seed: int, nb: int, stream=None):
+    """Synthetic orbital coefficients: Q of the Householder QR of the seeded N(0,1) matrix.
+
+    The seed matrix is generated on the device; the QR factorisation (input
+    preparation only) runs on the host through numpy's LAPACK.
+    """
+    import torch
+
+    M = torch.empty(nb * nb, dtype=torch.float64, device="cuda")
+    _check(lib().rt_synth_coef_seed(seed, nb, _dptr(M), _stream(stream)))
+    Mh = M.cpu().numpy().reshape(nb, nb, order="F")
+    Q, _ = np.linalg.qr(Mh)
+    return torch.from_numpy(np.ascontiguousarray(Q.reshape(-1, order="F"))).to(M.device)
+
+
+PROF_OZ_GEMM, PROF_OZ_SLICE, PROF_DGEMM, PROF_RIJ = 0, 1, 2, 3
+
+
+def launch_count() -> int:
+    return int(lib().rt_launch_count())
+
+
+def profile_enable(on: bool) -> None:
+    lib().rt_profile_enable(1 if on else 0)
+
+
+def profile_get(kind: int):
+    """(total event milliseconds, launches, algorithmic work) recorded for a kernel kind."""
+    ms, n, w = ctypes.c_double(), ctypes.c_longlong(), ctypes.c_double()
+    _check(lib().rt_profile_get(kind, ctypes.byref(ms), ctypes.byref(n), ctypes.byref(w)))
+    return ms.value, n.value, w.value
 
 
 def sync_status(stream=None) -> None:

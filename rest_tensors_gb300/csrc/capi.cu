@@ -12,6 +12,7 @@ namespace rt {
 rt_status ri_j_fp64(const double* B, const double* D, int nb, int naux, double* w, double* J, cudaStream_t stream);
 rt_status exchange_energy(const double* D, const double* K, int nb, double* out, cudaStream_t stream);
 rt_status synth_ri3ao(uint64_t seed, int nb, int P0, int nslab, double* B, cudaStream_t stream);
+rt_status synth_coef_seed(uint64_t seed, int nb, double* M, cudaStream_t stream);
 rt_status ri_ao2mo_fp64(const double* C, const double* B, double* R, int nb, int ns, int naux, cudaStream_t stream);
 rt_status ri_ov_k_fp64(const double* C, const double* B, int nb, int naux, int nocc, int nvir, double* ov,
                        double* K, cudaStream_t stream);
@@ -131,6 +132,39 @@ rt_status rt_dgemm(char opa, char opb, int m, int n, int k, double alpha, const 
     return gemm_f64(g, (cudaStream_t)stream);
 }
 
+rt_status rt_dgemm_split(char opa, char opb, int m, int n, int k, const double* A, int lda, const double* B, int ldb,
+                         double* C, int ldc, int nslices, void* stream) {
+    RT_REQUIRE(m >= 0 && n >= 0 && k >= 0, "rt_dgemm_split: negative dimension");
+    RT_REQUIRE(opa == 'N' || opa == 'T', "rt_dgemm_split: opa must be N or T");
+    RT_REQUIRE(opb == 'N' || opb == 'T', "rt_dgemm_split: opb must be N or T");
+    RT_REQUIRE(nslices >= 3 && nslices <= 8, "rt_dgemm_split: nslices must be in 3..8");
+    RT_REQUIRE(lda >= std::max(1, opa == 'N' ? m : k), "rt_dgemm_split: lda too small");
+    RT_REQUIRE(ldb >= std::max(1, opb == 'N' ? k : n), "rt_dgemm_split: ldb too small");
+    RT_REQUIRE(ldc >= std::max(1, m), "rt_dgemm_split: ldc too small");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (m == 0 || n == 0) return RT_OK;
+    if (k == 0) {
+        RT_CUDA_TRY(cudaMemset2DAsync(C, sizeof(double) * ldc, 0, sizeof(double) * m, n, s));
+        return RT_OK;
+    }
+    OzGemm g;
+    g.K = k;
+    // C(i, j) = sum_k opA(i, k) opB(k, j), written as sum_k A'(i, k) B'(j, k)
+    g.A.p = A; g.A.rows = m;
+    if (opa == 'N') { g.A.s0 = 1; g.A.sk = lda; } else { g.A.s0 = lda; g.A.sk = 1; }
+    g.B.p = B; g.B.rows = n;
+    if (opb == 'N') { g.B.s0 = ldb; g.B.sk = 1; } else { g.B.s0 = 1; g.B.sk = ldb; }
+    g.C.p = C; g.C.ms0 = 1; g.C.ns0 = ldc;
+    g.nslices = nslices;
+    // A * A^T (same matrix on both sides): slice once and compute one triangle.
+    if (A == B && opa != opb && lda == ldb && m == n) {
+        g.B = g.A;
+        g.b_is_a = true;
+        g.symmetric = true;
+    }
+    return oz_gemm(g, s);
+}
+
 rt_status rt_ri_ao2mo(const double* C, const double* B, double* ri3mo, int nb, int ns, int naux, int form,
                       int nslices, void* stream) {
     RT_REQUIRE(nb >= 0 && ns >= 0 && naux >= 0, "rt_ri_ao2mo: negative dimension");
@@ -180,6 +214,11 @@ rt_status rt_ri_exchange_energy(const double* D, const double* K, int nb, double
 rt_status rt_synth_ri3ao(uint64_t seed, int nb, int P0, int nslab, double* B, void* stream) {
     RT_REQUIRE(nb >= 0 && P0 >= 0 && nslab >= 0, "rt_synth_ri3ao: negative argument");
     return synth_ri3ao(seed, nb, P0, nslab, B, (cudaStream_t)stream);
+}
+
+rt_status rt_synth_coef_seed(uint64_t seed, int nb, double* M, void* stream) {
+    RT_REQUIRE(nb >= 0, "rt_synth_coef_seed: negative size");
+    return synth_coef_seed(seed, nb, M, (cudaStream_t)stream);
 }
 
 rt_status rt_ri_ov_k_host(const double* C, const double* B, int nb, int naux, int nocc, int nvir, double* ov,

@@ -173,10 +173,12 @@ rt_status gemm_f64(const GemmF64& q, cudaStream_t stream) {
     }
     dim3 grid((unsigned)(g.tiles_m * g.tiles_n), (unsigned)(q.batch < 65535 ? q.batch : 65535), (unsigned)splitk);
     const bool ta = q.opa == 'T', tb = q.opb == 'T';
+    prof_begin(PROF_DGEMM, stream);
     if (!ta && !tb) dgemm_tile_kernel<false, false><<<grid, NT, 0, stream>>>(g);
     else if (ta && !tb) dgemm_tile_kernel<true, false><<<grid, NT, 0, stream>>>(g);
     else if (!ta && tb) dgemm_tile_kernel<false, true><<<grid, NT, 0, stream>>>(g);
     else dgemm_tile_kernel<true, true><<<grid, NT, 0, stream>>>(g);
+    prof_end(PROF_DGEMM, stream, 2.0 * (double)q.m * (double)q.n * (double)q.k * (double)q.batch);
     RT_TRY(check_launch("dgemm_tile_kernel"));
     if (splitk > 1) {
         dgemm_splitk_reduce<<<2 * sm_count(), 256, 0, stream>>>(g);
@@ -292,6 +294,13 @@ __global__ void __launch_bounds__(1024) exchange_kernel(const double* __restrict
     }
 }
 
+__global__ void synth_coef_kernel(uint64_t seed, int nb, double* M) {
+    const int64_t total = (int64_t)nb * nb;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x)
+        M[idx] = rt_coef_seed_elem(seed, idx % nb, idx / nb);
+}
+
 __global__ void synth_kernel(uint64_t seed, int nb, int P0, int64_t total, double* B) {
     const int64_t nb2 = (int64_t)nb * nb;
     for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
@@ -336,6 +345,12 @@ rt_status synth_ri3ao(uint64_t seed, int nb, int P0, int nslab, double* B, cudaS
     if (total == 0) return RT_OK;
     synth_kernel<<<8 * sm_count(), 256, 0, stream>>>(seed, nb, P0, total, B);
     return check_launch("synth_kernel");
+}
+
+rt_status synth_coef_seed(uint64_t seed, int nb, double* M, cudaStream_t stream) {
+    if (nb <= 0) return RT_OK;
+    synth_coef_kernel<<<sm_count(), 256, 0, stream>>>(seed, nb, M);
+    return check_launch("synth_coef_kernel");
 }
 
 // Plain-form AO->MO transform: T^P = B^P C, then R^P = C^T T^P stored P-fastest.

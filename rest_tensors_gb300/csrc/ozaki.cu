@@ -8,7 +8,7 @@
 //  * Every row of A (and of B, both stored "K-contiguous": C = A B^T) gets a
 //    power-of-two scale from its largest exponent.  Each element is turned,
 //    with integer operations only, into S signed base-128 digits d_0..d_{S-1}
-//    (|d| <= 65, rounded to nearest at the last digit):
+//    (|d| <= 65, rounded to nearest-even at the last digit):
 //        x ~= 2^(e_row - 1028) * sum_s d_s 2^(-7 s)
 //    Small integers are exact in BF16, so each digit plane is a BF16 matrix.
 //  * Digit planes are multiplied pairwise on tcgen05 (kind::f16, BF16 in,
@@ -20,8 +20,9 @@
 //    (their weight is below the last digit's).
 //  * The epilogue converts each G_g to an integer, forms
 //        V = sum_g G_g 2^(7 (S - 1 - g) - R)
-//    exactly in int64 (R is a right shift that keeps V in range across all
-//    chunks), and rounds once to float64:
+//    in int64 (R, a right shift with round-half-even, keeps V in range over
+//    the chunks one CTA accumulates; split-K partials are summed in 128 bits),
+//    and rounds once to float64:
 //        C = V * 2^(eA + eB - 2056 - 7 (S - 1) + R).
 //
 // GB300 runs float64 arithmetic at ~1.2 TFLOP/s, so everything above is
@@ -33,6 +34,7 @@
 // core matrices), pre-tiled as [tile][k-block][digit][T rows x 32 k], so one
 // pipeline stage is a handful of 1-D bulk copies (cp.async.bulk) per operand.
 #include <algorithm>
+#include <cmath>
 
 #include "rt_internal.cuh"
 #include "rt_ptx.cuh"
@@ -79,8 +81,9 @@ struct SliceArgs {
 
 template <int S>
 struct DigitConst {
-    // q has the row maximum's leading bit at position 61; digit s sits at bit 56 - 7 s.
-    static constexpr unsigned long long rnd = 1ull << (55 - 7 * (S - 1));
+    // q has the row maximum's leading bit at position 61; digit s sits at bit
+    // 56 - 7 s, so the last digit's unit is 2^L.
+    static constexpr int L = 56 - 7 * (S - 1);
     static constexpr unsigned long long off() {
         unsigned long long o = 0;
         for (int k = 1; k < S; ++k) o += 1ull << (62 - 7 * k);
@@ -89,23 +92,27 @@ struct DigitConst {
 };
 
 // Signed base-128 digits of x relative to the row exponent emax (biased).
+// The last digit is rounded to nearest, ties to even; mantissa bits shifted
+// out below q are kept as a sticky bit, so only true ties go to even.  (Ties
+// are common when x is itself the output of this GEMM, whose results lie on a
+// coarse power-of-two grid; rounding ties away from zero would then bias |x|
+// upward.)
 template <int S>
 __device__ __forceinline__ void split_digits(double x, int emax, int (&d)[S]) {
     const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
     const int e = (int)((bits >> 52) & 0x7FF);
     const int sh = emax - e + 1;
-    unsigned long long q = 0;
-    if (e != 0 && sh < 64) {
-        const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-        q = (mant << 10) >> sh;
-    }
-    const unsigned long long t = q + (q ? (DigitConst<S>::rnd + DigitConst<S>::off()) : 0ull);
-    const bool neg = (bits >> 63) != 0;
-    if (q == 0) {
+    if (e == 0 || sh >= 64) {
 #pragma unroll
         for (int s = 0; s < S; ++s) d[s] = 0;
         return;
     }
+    const unsigned long long full = ((bits & 0xFFFFFFFFFFFFFull) | (1ull << 52)) << 10;
+    unsigned long long q = full >> sh;
+    q |= (full & ((1ull << sh) - 1ull)) != 0ull ? 1ull : 0ull;
+    constexpr int L = DigitConst<S>::L;
+    const unsigned long long t = q + ((1ull << (L - 1)) - 1ull) + ((q >> L) & 1ull) + DigitConst<S>::off();
+    const bool neg = (bits >> 63) != 0;
     d[0] = (int)(t >> 56);
 #pragma unroll
     for (int s = 1; s < S; ++s) d[s] = (int)((t >> (56 - 7 * s)) & 127ull) - 64;
@@ -299,7 +306,6 @@ __global__ void __launch_bounds__(NTHREADS, 1) oz_gemm_kernel(GemmArgs a) {
     constexpr uint32_t A_STAGE = S * A_BLK;
     constexpr uint32_t STAGE = S * (A_BLK + B_BLK);
     constexpr uint32_t NCOLS = tmem_cols(S);
-    constexpr uint32_t IDESC = ptx::idesc_bf16_f32(TM, TN);
 
     extern __shared__ __align__(1024) uint8_t smem[];
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE);
@@ -387,16 +393,22 @@ __global__ void __launch_bounds__(NTHREADS, 1) oz_gemm_kernel(GemmArgs a) {
                     ptx::tc_fence_after();
                     const uint32_t sa = sbase + st * STAGE;
                     const uint32_t sb = sa + A_STAGE;
+                    // For digit s of A, the B digit planes t = 0 .. S-1-s sit back to back in
+                    // shared memory and form one K-major operand of 64*(S-s) rows; their
+                    // products land in adjacent accumulator groups s .. S-1.  One MMA with
+                    // N = 64*(S-s) (split at 256) therefore covers all pairs of digit s.
 #pragma unroll
                     for (int s = 0; s < S; ++s) {
 #pragma unroll
-                        for (int t = 0; t < S - s; ++t) {
+                        for (int t0 = 0; t0 < S - s; t0 += 4) {
+                            const int nt = (S - s - t0) < 4 ? (S - s - t0) : 4;
+                            const uint32_t idesc = ptx::idesc_bf16_f32(TM, TN * nt);
 #pragma unroll
                             for (int kk = 0; kk < KB / 16; ++kk) {
                                 const uint64_t ad = ptx::smem_desc_kmajor_noswizzle(sa + s * A_BLK + kk * 256, 128, 512);
-                                const uint64_t bd = ptx::smem_desc_kmajor_noswizzle(sb + t * B_BLK + kk * 256, 128, 512);
+                                const uint64_t bd = ptx::smem_desc_kmajor_noswizzle(sb + t0 * B_BLK + kk * 256, 128, 512);
                                 const uint32_t acc = (first && kk == 0 && s == 0) ? 0u : 1u;
-                                ptx::mma_bf16_ss(tmem + (uint32_t)((s + t) * TN), ad, bd, IDESC, acc);
+                                ptx::mma_bf16_ss(tmem + (uint32_t)((s + t0) * TN), ad, bd, idesc, acc);
                             }
                         }
                     }
@@ -432,7 +444,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) oz_gemm_kernel(GemmArgs a) {
 #pragma unroll
                     for (int j = 0; j < 16; ++j) {
                         const int64_t v = (int64_t)__float2int_rn(__uint_as_float(r[j]));
-                        acc[cb * 16 + j] += sh >= 0 ? (v << sh) : ((v + (1ll << (-sh - 1))) >> (-sh));
+                        // Right shifts round to nearest, ties to even.
+                        acc[cb * 16 + j] += sh >= 0 ? (v << sh)
+                                                    : ((v + (1ll << (-sh - 1)) - 1 + ((v >> (-sh)) & 1)) >> (-sh));
                     }
                 }
             }
@@ -466,7 +480,25 @@ __global__ void __launch_bounds__(NTHREADS, 1) oz_gemm_kernel(GemmArgs a) {
     }
 }
 
-// Sum split-K int64 partials (exact, order-free) and round once to float64.
+// Correctly rounded float64 of a signed 128-bit integer times 2^ex.
+__device__ __forceinline__ double scale_pow2_i128(__int128 v, int ex) {
+    if (v == 0) return 0.0;
+    const bool neg = v < 0;
+    unsigned __int128 a = neg ? (unsigned __int128)(-v) : (unsigned __int128)v;
+    int s = 0;
+    // Bring |v| below 2^63 keeping a sticky bit; 10+ guard bits remain above
+    // the 53-bit significand, so the final conversion rounds correctly.
+    while ((a >> 63) != 0) {
+        const unsigned __int128 lost = a & 1;
+        a >>= 1;
+        a |= lost;
+        ++s;
+    }
+    const int64_t w = neg ? -(int64_t)a : (int64_t)a;
+    return scale_pow2(w, ex + s);
+}
+
+// Sum split-K int64 partials exactly in 128 bits and round once to float64.
 template <int S>
 __global__ void oz_finalize_kernel(GemmArgs a) {
     const int64_t ldp = a.tiles_n * TN;
@@ -475,10 +507,10 @@ __global__ void oz_finalize_kernel(GemmArgs a) {
          idx += (int64_t)gridDim.x * blockDim.x) {
         const int64_t n = idx / a.M, m = idx % a.M;
         if (a.symmetric && n < m) continue;
-        int64_t v = 0;
-        for (int z = 0; z < a.splits; ++z) v += a.partial[((int64_t)z * a.tiles_m * TM + m) * ldp + n];
+        __int128 v = 0;
+        for (int z = 0; z < a.splits; ++z) v += (__int128)a.partial[((int64_t)z * a.tiles_m * TM + m) * ldp + n];
         const int ex = a.ea[m] + a.eb[n] - 2056 - 7 * (S - 1) + a.R;
-        a.out.p[out_addr(a.out, m, n)] = scale_pow2(v, ex);
+        a.out.p[out_addr(a.out, m, n)] = scale_pow2_i128(v, ex);
     }
 }
 
@@ -550,9 +582,13 @@ rt_status run(const OzGemm& g, cudaStream_t stream) {
     Operand A{g.A.p, g.A.rows, g.A.div, g.A.s0, g.A.s1, g.A.sk};
     Operand B{g.B.p, g.B.rows, g.B.div, g.B.s0, g.B.s1, g.B.sk};
     Sliced sa, sb;
-    RT_TRY(slice_operand<S>(A, g.K, TM, sa, stream));
     const bool reuse = g.b_is_a;
+    // Slicing is HBM-bound: count bytes (8 read + 2*S written per element).
+    const double slice_bytes = (double)(A.rows + (reuse ? 0 : B.rows)) * (double)g.K * (8.0 + 2.0 * S);
+    prof_begin(PROF_OZ_SLICE, stream);
+    RT_TRY(slice_operand<S>(A, g.K, TM, sa, stream));
     if (!reuse) RT_TRY(slice_operand<S>(B, g.K, TN, sb, stream));
+    prof_end(PROF_OZ_SLICE, stream, slice_bytes);
 
     GemmArgs a{};
     a.a_slices = sa.planes.as<uint8_t>();
@@ -586,18 +622,38 @@ rt_status run(const OzGemm& g, cudaStream_t stream) {
     a.out = OutMap{g.C.p, g.C.md, g.C.ms0, g.C.ms1, g.C.nd, g.C.ns0, g.C.ns1};
     a.err = error_word_device();
 
-    // Split the chunk range across CTAs when there are too few tiles to fill the GPU.
+    // Split the chunk range across CTAs when there are too few tiles to fill the
+    // GPU; pick the split count whose CTA total best fills whole waves.
     const int64_t tiles = a.tiles_m * a.tiles_n;
+    int64_t active = tiles;
+    if (g.symmetric) {
+        active = 0;
+        for (int64_t tm = 0; tm < a.tiles_m; ++tm)
+            for (int64_t tn = 0; tn < a.tiles_n; ++tn)
+                if (tn * TN + TN - 1 >= tm * TM) ++active;
+    }
     int64_t splits = 1;
-    const int64_t want = sm_count();
-    if (tiles < want && a.nchunks > 1) splits = std::min<int64_t>(a.nchunks, ceil_div(want, tiles));
+    const int64_t sms = sm_count();
+    if (active < sms && a.nchunks > 1) {
+        double best = 0.0;
+        for (int64_t w = 1; w <= 4; ++w) {
+            const int64_t sp = std::min<int64_t>(a.nchunks, std::max<int64_t>(1, (w * sms) / active));
+            const double eff = (double)(active * sp) / (double)(ceil_div(active * sp, sms) * sms);
+            if (eff > best + 0.02) { best = eff; splits = sp; }
+        }
+    }
     a.chunks_per_split = (int)ceil_div(a.nchunks, splits);
     splits = ceil_div(a.nchunks, a.chunks_per_split);
     a.splits = (int)splits;
-    // |G_g| < 2^24; V per chunk < 2^(24 + 7(S-1) - R + 0.02); sum over all chunks must stay < 2^62.
-    int lg = 0;
-    while ((1ll << lg) < a.nchunks) ++lg;
-    a.R = std::max(0, 24 + 7 * (S - 1) + 1 + lg - 62);
+    // Overflow guard for the int64 accumulator of one CTA: over n contraction
+    // terms, |V| <= n * 65^2 * 2^(7(S-1)-R) * sum_g (g+1) 2^(-7g) < n * 4292 * 2^(7(S-1)-R),
+    // kept below 2^62.  Split-K partials are summed in 128 bits, so only the
+    // terms one CTA sees count.
+    {
+        const double terms = (double)a.chunks_per_split * a.chunk_kb * KB;
+        const int need = (int)std::ceil(std::log2(terms * 4292.0)) + 7 * (S - 1) - 62;
+        a.R = std::max(0, need);
+    }
 
     ScratchBuf part;
     if (splits > 1) {
@@ -606,7 +662,12 @@ rt_status run(const OzGemm& g, cudaStream_t stream) {
     }
     constexpr int smem = num_stages(S) * stage_bytes(S) + 256;
     dim3 grid((unsigned)tiles, (unsigned)splits);
+    // Algorithmic tensor work: S(S+1)/2 digit-pair products of 2*M*N*K each
+    // (half of the square for the symmetric product).
+    const double pair_flops = 2.0 * (double)a.M * (double)a.N * (double)g.K * (g.symmetric ? 0.5 : 1.0);
+    prof_begin(PROF_OZ_GEMM, stream);
     oz_gemm_kernel<S><<<grid, NTHREADS, smem, stream>>>(a);
+    prof_end(PROF_OZ_GEMM, stream, pair_flops * S * (S + 1) / 2);
     RT_TRY(check_launch("oz_gemm_kernel"));
     if (splits > 1) {
         oz_finalize_kernel<S><<<4 * sm_count(), 256, 0, stream>>>(a);

@@ -4,7 +4,9 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <atomic>
 #include <mutex>
+#include <vector>
 
 #include "rt_internal.cuh"
 
@@ -23,7 +25,10 @@ void set_error(rt_status s, const char* fmt, ...) {
 
 rt_status last_status() { return g_last_status; }
 
+static std::atomic<long long> g_launches{0};
+
 rt_status check_launch(const char* what) {
+    g_launches.fetch_add(1, std::memory_order_relaxed);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         set_error(RT_ERR_CUDA, "launch of %s failed: %s", what, cudaGetErrorString(e));
@@ -82,9 +87,73 @@ int sm_count() {
     return n;
 }
 
+// ---------------------------------------------------------------- profiler --
+namespace {
+struct ProfRec {
+    int kind;
+    cudaEvent_t a, b;
+    double flops;
+};
+std::mutex g_prof_mu;
+std::atomic<bool> g_prof_on{false};
+std::vector<ProfRec> g_prof_recs;
+thread_local cudaEvent_t g_prof_pending[PROF_NKINDS] = {};
+}  // namespace
+
+bool prof_enabled() { return g_prof_on.load(std::memory_order_relaxed); }
+
+void prof_begin(int kind, cudaStream_t s) {
+    if (!prof_enabled()) return;
+    cudaEvent_t a;
+    if (cudaEventCreate(&a) != cudaSuccess) return;
+    cudaEventRecord(a, s);
+    g_prof_pending[kind] = a;
+}
+
+void prof_end(int kind, cudaStream_t s, double flops) {
+    if (!prof_enabled() || !g_prof_pending[kind]) return;
+    cudaEvent_t b;
+    if (cudaEventCreate(&b) != cudaSuccess) return;
+    cudaEventRecord(b, s);
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    g_prof_recs.push_back(ProfRec{kind, g_prof_pending[kind], b, flops});
+    g_prof_pending[kind] = nullptr;
+}
+
 }  // namespace rt
 
 extern "C" {
+
+long long rt_launch_count(void) { return rt::g_launches.load(); }
+
+void rt_profile_enable(int on) {
+    std::lock_guard<std::mutex> lk(rt::g_prof_mu);
+    for (auto& r : rt::g_prof_recs) {
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+    }
+    rt::g_prof_recs.clear();
+    rt::g_prof_on.store(on != 0);
+}
+
+rt_status rt_profile_get(int kind, double* total_ms, long long* launches, double* flops) {
+    std::lock_guard<std::mutex> lk(rt::g_prof_mu);
+    double ms = 0.0, fl = 0.0;
+    long long n = 0;
+    for (auto& r : rt::g_prof_recs) {
+        if (r.kind != kind) continue;
+        RT_CUDA_TRY(cudaEventSynchronize(r.b));
+        float t = 0.f;
+        RT_CUDA_TRY(cudaEventElapsedTime(&t, r.a, r.b));
+        ms += t;
+        fl += r.flops;
+        ++n;
+    }
+    if (total_ms) *total_ms = ms;
+    if (launches) *launches = n;
+    if (flops) *flops = fl;
+    return RT_OK;
+}
 
 int rt_version(void) { return (1 << 16) | 0; }
 

@@ -41,8 +41,16 @@ rt_status last_status();
         }                                                      \
     } while (0)
 
-// Check for a launch error right after a <<<>>> launch.
+// Check for a launch error right after a <<<>>> launch (also counts launches).
 rt_status check_launch(const char* what);
+
+// Opt-in kernel timing: when enabled, prof_begin/prof_end bracket a launch
+// with CUDA events on its stream and attribute `flops` algorithmic
+// operations to the kernel kind.
+enum ProfKind : int { PROF_OZ_GEMM = 0, PROF_OZ_SLICE = 1, PROF_DGEMM = 2, PROF_RIJ = 3, PROF_NKINDS = 4 };
+bool prof_enabled();
+void prof_begin(int kind, cudaStream_t s);
+void prof_end(int kind, cudaStream_t s, double flops);
 
 // Stream-ordered scratch from the device's default memory pool
 // (cudaMallocAsync / cudaFreeAsync on the call's stream), released when the

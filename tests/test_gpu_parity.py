@@ -218,3 +218,45 @@ def test_device_synth_matches_host_formula():
     ref = oracle.synth_ri3ao(7, nb, naux)
     got = host(rt.synth_ri3ao(7, nb, naux), (nb, nb, naux))
     assert np.max(np.abs(got - ref)) < 1e-14
+
+
+# ------------------------------------------------ split GEMM exactness --
+@pytest.mark.parametrize("opa,opb", [("N", "N"), ("T", "N"), ("N", "T"), ("T", "T")])
+@pytest.mark.parametrize("S", [5, 7, 8])
+def test_split_gemm_is_exact_on_short_integers(opa, opb, S):
+    """Integers of at most 20 significant bits need only digits 0..2; every
+    dropped digit pair is then zero, the float64 products are exact, and the
+    split form must reproduce them bit for bit (the exact-accumulation claim)."""
+    rng = np.random.default_rng(S)
+    m, n, k = 200, 130, 1500  # k spans three exact chunks at S = 7
+    A = rng.integers(-(2 ** 19), 2 ** 19, size=(m, k) if opa == "N" else (k, m)).astype(np.float64)
+    B = rng.integers(-(2 ** 19), 2 ** 19, size=(k, n) if opb == "N" else (n, k)).astype(np.float64)
+    # Give every row of op(A) and column of op(B) the same maximum exponent, so 20 bits fit in 3 digits.
+    A.flat[0::7] = 2.0 ** 19 - 1
+    B.flat[0::5] = -(2.0 ** 19 - 1)
+    A, B = np.asfortranarray(A), np.asfortranarray(B)
+    ref = (A if opa == "N" else A.T) @ (B if opb == "N" else B.T)
+    assert np.all(np.abs(ref) < 2.0 ** 52)  # exact in float64
+    dC = torch.zeros(m * n, dtype=torch.float64, device="cuda")
+    rt.dgemm_split(opa, opb, m, n, k, dev(A), A.shape[0], dev(B), B.shape[0], dC, m, nslices=S)
+    got = host(dC, (m, n))
+    assert np.array_equal(got, ref), float(np.max(np.abs(got - ref)))
+
+
+def test_split_rounding_has_no_bias_on_ties():
+    """Values on a 2^-48 grid with row maximum 1.5 put every odd multiple
+    exactly on a rounding tie of the last (7th) digit.  Ties must not all go
+    one way: the diagonal of X X^T must match the exact sum of squares with
+    no mean bias (ties rounded away from zero gave about +1e-14)."""
+    rng = np.random.default_rng(3)
+    nb, k = 64, 5000
+    J = np.clip(np.rint(rng.standard_normal((nb, k)) * 0.3 * 2.0 ** 48), -1.4 * 2 ** 48, 1.4 * 2 ** 48).astype(np.int64)
+    J[:, 0] = int(1.5 * 2 ** 48)
+    X = np.asfortranarray(J.astype(np.float64) * 2.0 ** -48)
+    dX = dev(X)
+    K = torch.zeros(nb * nb, dtype=torch.float64, device="cuda")
+    rt.dgemm_split("N", "T", nb, nb, k, dX, nb, dX, nb, K, nb, nslices=7)
+    d = torch.diagonal(K.view(nb, nb)).cpu().numpy()
+    exact = [sum(int(j) * int(j) for j in J[i].tolist()) for i in range(nb)]
+    rel = np.array([(d[i] * 2.0 ** 96 - exact[i]) / exact[i] for i in range(nb)])
+    assert abs(rel.mean()) < 2e-15 and np.max(np.abs(rel)) < 1e-13
