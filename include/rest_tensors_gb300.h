@@ -121,6 +121,20 @@ rt_status rt_ri_ao2mo(const double* C, const double* B, double* ri3mo, int nb, i
 rt_status rt_ri_ov_k(const double* C, const double* B, int nb, int naux, int nocc, int nvir, double* ov, double* K,
                      int form, int nslices, void* stream);
 
+/* Allocation-free float64 form of rt_ri_ov_k, for callers that cannot
+ * allocate device memory while they run (inside a stream capture that must
+ * hold no allocation nodes, under a fixed external memory arena, or on a
+ * serving path where cudaMalloc/cudaFree and their implicit synchronisation
+ * are not allowed).  It has no counterpart in the reference.  The half-
+ * transform goes through one fixed 32 MiB device array that the library
+ * holds on every GPU that loads it, so nb*nocc may be at most 4,194,304
+ * (larger requests fail with RT_ERR_INVALID_ARG); the aux slabs stream through
+ * it in blocks.  The first call on each device looks up the array's address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls share the array: calls whose kernels overlap on the GPU race. */
+rt_status rt_ri_ov_k_fp64_noalloc(const double* C, const double* B, int nb, int naux, int nocc, int nvir, double* ov,
+                                  double* K, void* stream);
+
 /* RI-J: w[P] = sum_{mu,nu} B^P[mu,nu] D[mu,nu] ("ip,ip->p", _einsum_02,
  * src/matrix/matrix_blas_lapack.rs:1293-1310 on the [nb*nb, naux] view of
  * ri.rs:309-316) and J = sum_P w[P] B^P.  w may be NULL. */

@@ -6,6 +6,9 @@
 // register-tiled DFMA GEMM service (batched, strided, optional split-K) on
 // which every contraction is composed, plus two DFMA streaming kernels for
 // RI-J and a fixed-order reduction for the exchange energy.
+#include <algorithm>
+#include <mutex>
+
 #include "rt_internal.cuh"
 #include "../../include/rt_synth.h"
 
@@ -417,3 +420,122 @@ rt_status ri_ov_k_fp64(const double* C, const double* B, int nb, int naux, int n
 }
 
 }  // namespace rt
+
+// ---------------------------------------------------------------------------
+// Allocation-free float64 ov transform + RI-K.
+//
+// For callers that cannot allocate device memory while they run: code that
+// executes inside a CUDA stream capture that must not contain allocation
+// nodes, hosts that hand the GPU's memory to a fixed arena managed by another
+// runtime, or deployments where any cudaMalloc/cudaFree (with its implicit
+// device synchronisation) is forbidden on the serving path.  The half-
+// transform X^P = B^P C_occ lives in a fixed file-scope device array instead
+// of scratch from the memory pool, and the aux slabs stream through it in
+// blocks; K accumulates across blocks with beta = 1.  Nothing in the array
+// needs to start at zero (every block's X is fully written before it is
+// read).  Every call shares the array, so calls whose kernels overlap on the
+// GPU (different streams, or different host threads) race on it.
+// ---------------------------------------------------------------------------
+
+namespace rt {
+namespace {
+
+constexpr size_t kNoAllocScratchDoubles = (size_t)4 << 20;  // 32 MiB
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles];
+
+// Device address of the array, looked up once per device.
+rt_status noalloc_scratch_address(double** out) {
+    static std::mutex mu;
+    static double* addr[64] = {};
+    int dev = 0;
+    RT_CUDA_TRY(cudaGetDevice(&dev));
+    RT_REQUIRE(dev >= 0 && dev < 64, "rt_ri_ov_k_fp64_noalloc: device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> lk(mu);
+    if (!addr[dev]) {
+        double* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress((void**)&p, g_noalloc_scratch);
+        if (e != cudaSuccess || p == nullptr) {
+            set_error(RT_ERR_CUDA, "rt_ri_ov_k_fp64_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+            return RT_ERR_CUDA;
+        }
+        addr[dev] = p;
+    }
+    *out = addr[dev];
+    return RT_OK;
+}
+
+// One dgemm_tile_kernel launch without split-K partials or profiling events.
+rt_status launch_dgemm_noalloc(const GemmF64& q, cudaStream_t stream) {
+    if (q.m == 0 || q.n == 0 || q.batch == 0) return RT_OK;
+    GemmArgs g{};
+    g.m = q.m; g.n = q.n; g.k = q.k; g.alpha = q.alpha; g.beta = q.beta;
+    g.A = q.A; g.lda = q.lda; g.sA = q.sA; g.B = q.B; g.ldb = q.ldb; g.sB = q.sB;
+    g.C = q.C; g.rsC = q.rsC; g.csC = q.csC; g.bsC = q.bsC; g.batch = q.batch;
+    g.tiles_m = ceil_div(q.m, BM);
+    g.tiles_n = ceil_div(q.n, BN);
+    g.splitk = 1;
+    g.kchunk = ceil_div(std::max<int64_t>(q.k, 1), BK) * BK;
+    if (q.k == 0) {
+        scale_kernel<<<1024, 256, 0, stream>>>(g);
+        return check_launch("scale_kernel");
+    }
+    dim3 grid((unsigned)(g.tiles_m * g.tiles_n), (unsigned)(q.batch < 65535 ? q.batch : 65535), 1u);
+    const bool ta = q.opa == 'T', tb = q.opb == 'T';
+    if (!ta && !tb) dgemm_tile_kernel<false, false><<<grid, NT, 0, stream>>>(g);
+    else if (ta && !tb) dgemm_tile_kernel<true, false><<<grid, NT, 0, stream>>>(g);
+    else if (!ta && tb) dgemm_tile_kernel<false, true><<<grid, NT, 0, stream>>>(g);
+    else dgemm_tile_kernel<true, true><<<grid, NT, 0, stream>>>(g);
+    return check_launch("dgemm_tile_kernel");
+}
+
+}  // namespace
+}  // namespace rt
+
+extern "C" rt_status rt_ri_ov_k_fp64_noalloc(const double* C, const double* B, int nb, int naux, int nocc, int nvir,
+                                             double* ov, double* K, void* stream) {
+    using namespace rt;
+    RT_REQUIRE(nb >= 0 && naux >= 0 && nocc >= 0 && nvir >= 0, "rt_ri_ov_k_fp64_noalloc: negative dimension");
+    const int64_t per = (int64_t)nb * nocc;
+    RT_REQUIRE((size_t)per <= kNoAllocScratchDoubles,
+               "rt_ri_ov_k_fp64_noalloc: nb*nocc = %lld exceeds the fixed scratch of %zu doubles (32 MiB)",
+               (long long)per, kNoAllocScratchDoubles);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (K && nb > 0 && (nocc == 0 || naux == 0))
+        RT_CUDA_TRY(cudaMemsetAsync(K, 0, sizeof(double) * nb * (size_t)nb, s));
+    if (per * naux == 0) {
+        if (ov && (int64_t)nocc * nvir * naux > 0)
+            RT_CUDA_TRY(cudaMemsetAsync(ov, 0, sizeof(double) * (size_t)nocc * nvir * naux, s));
+        return RT_OK;
+    }
+    RT_REQUIRE(C && B, "rt_ri_ov_k_fp64_noalloc: null input pointer");
+    double* X = nullptr;
+    RT_TRY(noalloc_scratch_address(&X));
+    const int64_t blk = std::min<int64_t>(naux, (int64_t)(kNoAllocScratchDoubles / (size_t)per));
+    for (int64_t P0 = 0; P0 < naux; P0 += blk) {
+        const int64_t np = std::min<int64_t>(blk, naux - P0);
+        GemmF64 g1;
+        g1.opa = 'N'; g1.opb = 'N'; g1.m = nb; g1.n = nocc; g1.k = nb;
+        g1.A = B + P0 * (int64_t)nb * nb; g1.lda = nb; g1.sA = (int64_t)nb * nb;
+        g1.B = C; g1.ldb = nb; g1.sB = 0;
+        g1.C = X; g1.rsC = 1; g1.csC = nb; g1.bsC = per; g1.batch = np;
+        RT_TRY(launch_dgemm_noalloc(g1, s));
+        if (ov && nvir > 0) {
+            GemmF64 g2;
+            g2.opa = 'T'; g2.opb = 'N'; g2.m = nocc; g2.n = nvir; g2.k = nb;
+            g2.A = X; g2.lda = nb; g2.sA = per;
+            g2.B = C + per; g2.ldb = nb; g2.sB = 0;
+            g2.C = ov + P0 * (int64_t)nocc * nvir; g2.rsC = 1; g2.csC = nocc; g2.bsC = (int64_t)nocc * nvir;
+            g2.batch = np;
+            RT_TRY(launch_dgemm_noalloc(g2, s));
+        }
+        if (K) {
+            GemmF64 g3;
+            g3.opa = 'N'; g3.opb = 'T'; g3.m = nb; g3.n = nb; g3.k = np * nocc;
+            g3.A = X; g3.lda = nb; g3.B = X; g3.ldb = nb;
+            g3.C = K; g3.rsC = 1; g3.csC = nb;
+            g3.beta = P0 == 0 ? 0.0 : 1.0;
+            RT_TRY(launch_dgemm_noalloc(g3, s));
+        }
+    }
+    return RT_OK;
+}
