@@ -44,8 +44,10 @@ namespace oz {
 
 constexpr int TM = 128;        // rows of A per tile (UMMA M)
 constexpr int TN = 64;         // rows of B per tile (UMMA N)
-constexpr int KB = 32;         // k elements per pipeline stage
-constexpr int NTHREADS = 192;  // warp 0 producer, warp 1 MMA, warps 2..5 epilogue
+constexpr int KB = 16;         // k elements per pipeline stage (one MMA k-step)
+constexpr int SK = 32;         // k elements one slicing CTA covers (two k-blocks)
+constexpr int NTHREADS = 320;  // warp 0 producer, warp 1 MMA, warps 2..9 epilogue
+constexpr int EPI_THREADS = 256;
 constexpr int kSmemBudget = 220 * 1024;
 
 __host__ __device__ constexpr int stage_bytes(int S) { return S * (TM + TN) * KB * 2; }
@@ -54,11 +56,19 @@ __host__ __device__ constexpr int num_stages(int S) {
 }
 // Longest contraction chunk whose group sums stay exact in FP32, in k-blocks.
 __host__ __device__ constexpr int chunk_kblocks(int S) { return (int)(((1 << 24) - 1) / (S * 65 * 65) / KB); }
+// Balanced chunking: the fewest exact chunks, of near-equal length.
+inline int64_t balanced_chunk_kb(int64_t Kb, int S) {
+    const int64_t n = ceil_div(Kb, chunk_kblocks(S));
+    return ceil_div(Kb, std::max<int64_t>(n, 1));
+}
 __host__ __device__ constexpr int tmem_cols(int S) { return S * TN <= 256 ? 256 : 512; }
 
-// Byte offset of element (r, k) inside one [T x 32] operand block.
+// Byte offset of element (r, k) inside one [T x 16] operand block: 8-row x
+// 16-byte core matrices, k-adjacent ones 128 B apart (LBO), row groups 256 B
+// apart (SBO).
+constexpr uint32_t kLBO = 128, kSBO = 256;
 __host__ __device__ __forceinline__ uint32_t core_offset(int r, int k) {
-    return (uint32_t)((r & 7) * 16 + (k & 7) * 2 + (k >> 3) * 128 + (r >> 3) * 512);
+    return (uint32_t)((r & 7) * 16 + (k & 7) * 2 + (k >> 3) * kLBO + (r >> 3) * kSBO);
 }
 
 struct Operand {
@@ -71,8 +81,8 @@ struct SliceArgs {
     int64_t K;
     int T;          // tile height (128 for A, 64 for B)
     int64_t tiles;  // ceil(rows / T)
-    int64_t Kb;     // ceil(K / 32)
-    uint16_t* out;  // [tiles][Kb][S][T*32]
+    int64_t Kb;     // ceil(K / 16)
+    uint16_t* out;  // [tiles][Kb][S][T*16]
     const int* emax;
     unsigned int* err;
 };
@@ -169,91 +179,88 @@ __global__ void emax_strided_kernel(Operand a, int64_t K, int64_t kspan, int* __
 
 // --------------------------------------------------------------- slicing --
 
-// Strided rows (s0 == 1): CTA = (tile, k-block); thread handles one row and
-// 32 / (256 / T) consecutive k, reading coalesced across consecutive rows.
+// Pack the S digit planes of 8 consecutive k of one row into 16-byte words.
 template <int S>
-__global__ void __launch_bounds__(256) slice_strided_kernel(SliceArgs a) {
-    const int T = a.T;
-    const int tpr = 256 / T;    // threads per row
-    const int kper = KB / tpr;  // consecutive k per thread (16 for T=128, 8 for T=64)
-    const int64_t tile = blockIdx.x;
-    const int64_t kb = blockIdx.y;
-    const int r = threadIdx.x % T;
-    const int kq = threadIdx.x / T;
-    const int64_t row = tile * T + r;
-    const bool valid = row < a.src.rows;
-    const int em = valid ? a.emax[row] : 0;
-    const double* base = valid ? a.src.p + (row % a.src.div) * a.src.s0 + (row / a.src.div) * a.src.s1 : nullptr;
-    uint16_t* blk = a.out + ((tile * a.Kb + kb) * S) * (int64_t)(T * KB);
-    for (int g = 0; g < kper; g += 8) {
-        uint32_t w[S][4];
+__device__ __forceinline__ void digits8(const double (&x)[8], int em, uint32_t (&w)[S][4]) {
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const int64_t k = kb * KB + kq * kper + g + j;
-            double x = 0.0;
-            if (valid && k < a.K) x = base[k * a.src.sk];
-            int d[S];
-            split_digits<S>(x, em, d);
-#pragma unroll
-            for (int s = 0; s < S; ++s) {
-                const uint32_t h = bf16_of_int(d[s]);
-                if (j & 1) w[s][j >> 1] |= h << 16;
-                else w[s][j >> 1] = h;
-            }
-        }
-        const int kk = kq * kper + g;
+    for (int j = 0; j < 8; ++j) {
+        int d[S];
+        split_digits<S>(x[j], em, d);
 #pragma unroll
         for (int s = 0; s < S; ++s) {
-            uint4 v = make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
-            *reinterpret_cast<uint4*>(reinterpret_cast<uint8_t*>(blk + (int64_t)s * T * KB) + core_offset(r, kk)) = v;
+            const uint32_t h = bf16_of_int(d[s]);
+            if (j & 1) w[s][j >> 1] |= h << 16;
+            else w[s][j >> 1] = h;
         }
     }
 }
 
-// Contiguous rows (sk == 1): CTA = (tile, k-block); the [T x 32] tile is
-// staged through shared memory with coalesced row reads, then sliced as above.
 template <int S>
-__global__ void __launch_bounds__(256) slice_contig_kernel(SliceArgs a) {
-    __shared__ double tileb[TM][KB + 1];
+__device__ __forceinline__ void store8(const SliceArgs& a, int64_t tile, int64_t kb, int r, int kk,
+                                       const uint32_t (&w)[S][4]) {
+    uint8_t* blk = reinterpret_cast<uint8_t*>(a.out + ((tile * a.Kb + kb) * S) * (int64_t)(a.T * KB));
+#pragma unroll
+    for (int s = 0; s < S; ++s)
+        *reinterpret_cast<uint4*>(blk + (int64_t)s * a.T * KB * 2 + core_offset(r, kk)) =
+            make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
+}
+
+// Strided rows (s0 == 1): CTA = (tile, 32 k); work item = (row, 8 consecutive
+// k), rows fastest, so reads are coalesced across consecutive rows.
+template <int S>
+__global__ void __launch_bounds__(256) slice_strided_kernel(SliceArgs a) {
     const int T = a.T;
     const int64_t tile = blockIdx.x;
-    const int64_t kb = blockIdx.y;
+    const int64_t k32 = blockIdx.y;
+    for (int item = threadIdx.x; item < T * (SK / 8); item += blockDim.x) {
+        const int r = item % T, q = item / T;
+        const int64_t kb = k32 * (SK / KB) + (q >> 1);
+        if (kb >= a.Kb) continue;
+        const int64_t row = tile * T + r;
+        const bool valid = row < a.src.rows;
+        const int em = valid ? a.emax[row] : 0;
+        const double* base = valid ? a.src.p + (row % a.src.div) * a.src.s0 + (row / a.src.div) * a.src.s1 : nullptr;
+        double x[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int64_t k = k32 * SK + q * 8 + j;
+            x[j] = (valid && k < a.K) ? base[k * a.src.sk] : 0.0;
+        }
+        uint32_t w[S][4];
+        digits8<S>(x, em, w);
+        store8<S>(a, tile, kb, r, (q & 1) * 8, w);
+    }
+}
+
+// Contiguous rows (sk == 1): the [T x 32] tile is staged through shared
+// memory with coalesced row reads, then sliced as above.
+template <int S>
+__global__ void __launch_bounds__(256) slice_contig_kernel(SliceArgs a) {
+    __shared__ double tileb[TM][SK + 1];
+    const int T = a.T;
+    const int64_t tile = blockIdx.x;
+    const int64_t k32 = blockIdx.y;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int rr = wid; rr < T; rr += 8) {
+    for (int rr = wid; rr < T; rr += blockDim.x / 32) {
         const int64_t row = tile * T + rr;
-        const int64_t k = kb * KB + lane;
+        const int64_t k = k32 * SK + lane;
         double x = 0.0;
         if (row < a.src.rows && k < a.K) x = a.src.p[(row % a.src.div) * a.src.s0 + (row / a.src.div) * a.src.s1 + k];
         tileb[rr][lane] = x;
     }
     __syncthreads();
-    const int tpr = 256 / T;
-    const int kper = KB / tpr;
-    const int r = threadIdx.x % T;
-    const int kq = threadIdx.x / T;
-    const int64_t row = tile * T + r;
-    const int em = row < a.src.rows ? a.emax[row] : 0;
-    uint16_t* blk = a.out + ((tile * a.Kb + kb) * S) * (int64_t)(T * KB);
-    for (int g = 0; g < kper; g += 8) {
+    for (int item = threadIdx.x; item < T * (SK / 8); item += blockDim.x) {
+        const int r = item % T, q = item / T;
+        const int64_t kb = k32 * (SK / KB) + (q >> 1);
+        if (kb >= a.Kb) continue;
+        const int64_t row = tile * T + r;
+        const int em = row < a.src.rows ? a.emax[row] : 0;
+        double x[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) x[j] = tileb[r][q * 8 + j];
         uint32_t w[S][4];
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const double x = tileb[r][kq * kper + g + j];
-            int d[S];
-            split_digits<S>(x, em, d);
-#pragma unroll
-            for (int s = 0; s < S; ++s) {
-                const uint32_t h = bf16_of_int(d[s]);
-                if (j & 1) w[s][j >> 1] |= h << 16;
-                else w[s][j >> 1] = h;
-            }
-        }
-        const int kk = kq * kper + g;
-#pragma unroll
-        for (int s = 0; s < S; ++s) {
-            uint4 v = make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
-            *reinterpret_cast<uint4*>(reinterpret_cast<uint8_t*>(blk + (int64_t)s * T * KB) + core_offset(r, kk)) = v;
-        }
+        digits8<S>(x, em, w);
+        store8<S>(a, tile, kb, r, (q & 1) * 8, w);
     }
 }
 
@@ -298,6 +305,25 @@ __device__ __forceinline__ int64_t out_addr(const OutMap& o, int64_t m, int64_t 
     return (m % o.md) * o.ms0 + (m / o.md) * o.ms1 + (n % o.nd) * o.ns0 + (n / o.nd) * o.ns1;
 }
 
+// Work item w of the persistent grid: tile (tm, tn) and split z; false if the
+// item has nothing to do (below the diagonal of a symmetric product, or an
+// empty chunk range).
+__device__ __forceinline__ bool work_item(const GemmArgs& a, int64_t w, int64_t& tm, int64_t& tn, int64_t& c0,
+                                          int64_t& c1, int& z) {
+    const int64_t tile = w / a.splits;
+    z = (int)(w % a.splits);
+    tn = tile % a.tiles_n;
+    tm = tile / a.tiles_n;
+    if (a.symmetric && (tn * TN + TN - 1) < tm * TM) return false;
+    c0 = (int64_t)z * a.chunks_per_split;
+    c1 = min(a.nchunks, c0 + a.chunks_per_split);
+    return c0 < c1;
+}
+
+// Persistent split-precision GEMM: one CTA per SM walks the work list with
+// stride gridDim.x.  Producer and MMA run ahead across tile boundaries; the
+// epilogue hands the tensor memory back as soon as it has read a chunk, so
+// the next chunk's MMAs overlap the previous tile's conversion and stores.
 template <int S>
 __global__ void __launch_bounds__(NTHREADS, 1) oz_gemm_kernel(GemmArgs a) {
     constexpr int STAGES = num_stages(S);
@@ -316,17 +342,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) oz_gemm_kernel(GemmArgs a) {
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t tn = blockIdx.x % a.tiles_n;
-    const int64_t tm = blockIdx.x / a.tiles_n;
-    const int split = blockIdx.y;
-    if (a.symmetric && (tn * TN + TN - 1) < tm * TM) return;  // strictly below the diagonal
-
-    const int64_t c0 = (int64_t)split * a.chunks_per_split;
-    const int64_t c1 = min(a.nchunks, c0 + a.chunks_per_split);
-    if (c0 >= c1) return;
-    const int64_t kb_begin = c0 * a.chunk_kb;
-    const int64_t kb_end = min(a.Kb, c1 * a.chunk_kb);
-    const int64_t nkb = kb_end - kb_begin;
+    const int64_t nitems = a.tiles_m * a.tiles_n * a.splits;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
@@ -334,7 +350,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) oz_gemm_kernel(GemmArgs a) {
             ptx::mbar_init(&empty[s], 1);
         }
         ptx::mbar_init(acc_full, 1);
-        ptx::mbar_init(acc_empty, 128);
+        ptx::mbar_init(acc_empty, EPI_THREADS);
         ptx::mbar_init(drain, 1);
         ptx::fence_mbar_init();
     }
@@ -352,20 +368,25 @@ __global__ void __launch_bounds__(NTHREADS, 1) oz_gemm_kernel(GemmArgs a) {
             // ---------------- producer: bulk copies of pre-tiled digit planes
             int64_t it = 0;
             bool ok = true;
-            const uint8_t* abase = a.a_slices + tm * a.a_tile_stride;
-            const uint8_t* bbase = a.b_slices + (tn >> 1) * a.b_tile2_stride + (tn & 1) * a.b_half_stride;
-            for (; it < nkb; ++it) {
-                const int st = (int)(it % STAGES);
-                const uint32_t ph = (uint32_t)((it / STAGES) & 1);
-                if (!ptx::mbar_wait(&empty[st], ph ^ 1u, a.err)) { ok = false; break; }
-                uint8_t* sa = smem + st * STAGE;
-                uint8_t* sb = sa + A_STAGE;
-                ptx::mbar_arrive_expect_tx(&full[st], STAGE);
-                const int64_t kb = kb_begin + it;
-                ptx::bulk_g2s(sa, abase + kb * a.a_kb_stride, A_STAGE, &full[st]);
+            for (int64_t w = blockIdx.x; w < nitems && ok; w += gridDim.x) {
+                int64_t tm, tn, c0, c1;
+                int z;
+                if (!work_item(a, w, tm, tn, c0, c1, z)) continue;
+                const uint8_t* abase = a.a_slices + tm * a.a_tile_stride;
+                const uint8_t* bbase = a.b_slices + (tn >> 1) * a.b_tile2_stride + (tn & 1) * a.b_half_stride;
+                const int64_t kb1 = min(a.Kb, c1 * a.chunk_kb);
+                for (int64_t kb = c0 * a.chunk_kb; kb < kb1; ++kb, ++it) {
+                    const int st = (int)(it % STAGES);
+                    const uint32_t ph = (uint32_t)((it / STAGES) & 1);
+                    if (!ptx::mbar_wait(&empty[st], ph ^ 1u, a.err)) { ok = false; break; }
+                    uint8_t* sa = smem + st * STAGE;
+                    uint8_t* sb = sa + A_STAGE;
+                    ptx::mbar_arrive_expect_tx(&full[st], STAGE);
+                    ptx::bulk_g2s(sa, abase + kb * a.a_kb_stride, A_STAGE, &full[st]);
 #pragma unroll
-                for (int s = 0; s < S; ++s)
-                    ptx::bulk_g2s(sb + s * B_BLK, bbase + kb * a.b_kb_stride + s * a.b_s_stride, B_BLK, &full[st]);
+                    for (int s = 0; s < S; ++s)
+                        ptx::bulk_g2s(sb + s * B_BLK, bbase + kb * a.b_kb_stride + s * a.b_s_stride, B_BLK, &full[st]);
+                }
             }
             if (!ok) {
                 // Let copies already issued land before the CTA can exit.
@@ -377,97 +398,112 @@ __global__ void __launch_bounds__(NTHREADS, 1) oz_gemm_kernel(GemmArgs a) {
         if (lane == 0) {
             // ---------------- MMA issuer
             bool ok = true;
-            int64_t it = 0;
+            int64_t it = 0, cc = 0;
             const uint32_t sbase = ptx::smem_u32(smem);
-            for (int64_t c = c0; c < c1 && ok; ++c) {
-                if (c > c0) {
-                    if (!ptx::mbar_wait(acc_empty, (uint32_t)((c - c0 - 1) & 1), a.err)) { ok = false; break; }
-                    ptx::tc_fence_after();
-                }
-                const int64_t cb_end = min(kb_end, (c + 1) * (int64_t)a.chunk_kb);
-                bool first = true;
-                for (int64_t kb = c * a.chunk_kb; kb < cb_end; ++kb, ++it) {
-                    const int st = (int)(it % STAGES);
-                    const uint32_t ph = (uint32_t)((it / STAGES) & 1);
-                    if (!ptx::mbar_wait(&full[st], ph, a.err)) { ok = false; break; }
-                    ptx::tc_fence_after();
-                    const uint32_t sa = sbase + st * STAGE;
-                    const uint32_t sb = sa + A_STAGE;
-                    // For digit s of A, the B digit planes t = 0 .. S-1-s sit back to back in
-                    // shared memory and form one K-major operand of 64*(S-s) rows; their
-                    // products land in adjacent accumulator groups s .. S-1.  One MMA with
-                    // N = 64*(S-s) (split at 256) therefore covers all pairs of digit s.
+            const uint64_t adesc0 = ptx::smem_desc_kmajor_noswizzle(sbase, kLBO, kSBO);
+            const uint64_t bdesc0 = ptx::smem_desc_kmajor_noswizzle(sbase + A_STAGE, kLBO, kSBO);
+            for (int64_t w = blockIdx.x; w < nitems && ok; w += gridDim.x) {
+                int64_t tm, tn, c0, c1;
+                int z;
+                if (!work_item(a, w, tm, tn, c0, c1, z)) continue;
+                for (int64_t c = c0; c < c1 && ok; ++c, ++cc) {
+                    if (cc > 0) {
+                        if (!ptx::mbar_wait(acc_empty, (uint32_t)((cc - 1) & 1), a.err)) { ok = false; break; }
+                        ptx::tc_fence_after();
+                    }
+                    const int64_t kb1 = min(a.Kb, (c + 1) * (int64_t)a.chunk_kb);
+                    bool first = true;
+                    for (int64_t kb = c * a.chunk_kb; kb < kb1; ++kb, ++it) {
+                        const int st = (int)(it % STAGES);
+                        const uint32_t ph = (uint32_t)((it / STAGES) & 1);
+                        if (!ptx::mbar_wait(&full[st], ph, a.err)) { ok = false; break; }
+                        ptx::tc_fence_after();
+                        // Descriptors differ between stages only in the start-address field
+                        // (bits 0-13, address >> 4), which never carries for shared memory.
+                        const uint64_t soff = (uint64_t)((st * STAGE) >> 4);
+                        // For digit s of A, the B digit planes t = 0 .. S-1-s sit back to back in
+                        // shared memory and form one K-major operand of 64*(S-s) rows; their
+                        // products land in adjacent accumulator groups s .. S-1.  One MMA with
+                        // N = 64*(S-s) (split at 256) therefore covers all pairs of digit s.
 #pragma unroll
-                    for (int s = 0; s < S; ++s) {
+                        for (int s = 0; s < S; ++s) {
 #pragma unroll
-                        for (int t0 = 0; t0 < S - s; t0 += 4) {
-                            const int nt = (S - s - t0) < 4 ? (S - s - t0) : 4;
-                            const uint32_t idesc = ptx::idesc_bf16_f32(TM, TN * nt);
-#pragma unroll
-                            for (int kk = 0; kk < KB / 16; ++kk) {
-                                const uint64_t ad = ptx::smem_desc_kmajor_noswizzle(sa + s * A_BLK + kk * 256, 128, 512);
-                                const uint64_t bd = ptx::smem_desc_kmajor_noswizzle(sb + t0 * B_BLK + kk * 256, 128, 512);
-                                const uint32_t acc = (first && kk == 0 && s == 0) ? 0u : 1u;
-                                ptx::mma_bf16_ss(tmem + (uint32_t)((s + t0) * TN), ad, bd, idesc, acc);
+                            for (int t0 = 0; t0 < S - s; t0 += 4) {
+                                const int nt = (S - s - t0) < 4 ? (S - s - t0) : 4;
+                                const uint32_t acc = (first && s == 0) ? 0u : 1u;
+                                ptx::mma_bf16_ss(tmem + (uint32_t)((s + t0) * TN), adesc0 + soff + (uint64_t)((s * A_BLK) >> 4),
+                                                 bdesc0 + soff + (uint64_t)((t0 * B_BLK) >> 4),
+                                                 ptx::idesc_bf16_f32(TM, TN * nt), acc);
                             }
                         }
+                        ptx::mma_commit(&empty[st]);
+                        first = false;
                     }
-                    ptx::mma_commit(&empty[st]);
-                    first = false;
+                    if (ok) ptx::mma_commit(acc_full);
                 }
-                if (ok) ptx::mma_commit(acc_full);
             }
             // Every MMA issued so far has completed once `drain` fires.
             ptx::mma_commit(drain);
             ptx::mbar_wait(drain, 0, a.err);
         }
     } else {
-        // ---------------- epilogue: 4 warps cover the 128 TMEM lanes
+        // ---------------- epilogue: 8 warps; warp w reads TMEM lane quadrant w % 4
+        // (its hardware-assigned lanes) and one half of the 64 columns.
+        constexpr int HC = TN / 2;
         const int q = warp & 3;
+        const int h = (warp - 2) >> 2;
         const int rl = 32 * q + lane;
-        const int64_t m = tm * TM + rl;
-        int64_t acc[TN];
-#pragma unroll
-        for (int j = 0; j < TN; ++j) acc[j] = 0;
+        int64_t cc = 0;
         bool ok = true;
-        for (int64_t c = c0; c < c1; ++c) {
-            if (!ptx::mbar_wait(acc_full, (uint32_t)((c - c0) & 1), a.err)) { ok = false; break; }
-            ptx::tc_fence_after();
+        for (int64_t w = blockIdx.x; w < nitems && ok; w += gridDim.x) {
+            int64_t tm, tn, c0, c1;
+            int z;
+            if (!work_item(a, w, tm, tn, c0, c1, z)) continue;
+            const int64_t m = tm * TM + rl;
+            int64_t acc[HC];
 #pragma unroll
-            for (int g = 0; g < S; ++g) {
-                const int sh = 7 * (S - 1 - g) - a.R;
-#pragma unroll
-                for (int cb = 0; cb < TN / 16; ++cb) {
-                    uint32_t r[16];
-                    ptx::tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(g * TN + cb * 16), r);
+            for (int j = 0; j < HC; ++j) acc[j] = 0;
+            for (int64_t c = c0; c < c1; ++c, ++cc) {
+                if (!ptx::mbar_wait(acc_full, (uint32_t)(cc & 1), a.err)) { ok = false; break; }
+                ptx::tc_fence_after();
+#pragma unroll 1
+                for (int g = 0; g < S; ++g) {
+                    const int sh = 7 * (S - 1 - g) - a.R;
+                    uint32_t r0[16], r1[16];
+                    const uint32_t col = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(g * TN + h * HC);
+                    ptx::tmem_ld16(col, r0);
+                    ptx::tmem_ld16(col + 16, r1);
                     ptx::tmem_wait_ld();
+                    if (sh >= 0) {
 #pragma unroll
-                    for (int j = 0; j < 16; ++j) {
-                        const int64_t v = (int64_t)__float2int_rn(__uint_as_float(r[j]));
+                        for (int j = 0; j < HC; ++j)
+                            acc[j] += (int64_t)__float2int_rn(__uint_as_float(j < 16 ? r0[j] : r1[j - 16])) << sh;
+                    } else {
                         // Right shifts round to nearest, ties to even.
-                        acc[cb * 16 + j] += sh >= 0 ? (v << sh)
-                                                    : ((v + (1ll << (-sh - 1)) - 1 + ((v >> (-sh)) & 1)) >> (-sh));
+                        const int r = -sh;
+                        const int64_t half = (1ll << (r - 1)) - 1;
+#pragma unroll
+                        for (int j = 0; j < HC; ++j) {
+                            const int64_t v = (int64_t)__float2int_rn(__uint_as_float(j < 16 ? r0[j] : r1[j - 16]));
+                            acc[j] += (v + half + ((v >> r) & 1)) >> r;
+                        }
                     }
                 }
+                ptx::tc_fence_before();
+                ptx::mbar_arrive(acc_empty);
             }
-            ptx::tc_fence_before();
-            ptx::mbar_arrive(acc_empty);
-        }
-        if (ok && m < a.M) {
+            if (!ok || m >= a.M) continue;
+            const int64_t n0 = tn * TN + h * HC;
             if (a.splits > 1) {
-                int64_t* dst = a.partial + ((int64_t)split * a.tiles_m * TM + m) * (a.tiles_n * TN) + tn * TN;
+                int64_t* dst = a.partial + ((int64_t)z * a.tiles_m * TM + m) * (a.tiles_n * TN) + n0;
 #pragma unroll
-                for (int j = 0; j < TN; ++j) dst[j] = acc[j];
+                for (int j = 0; j < HC; ++j) dst[j] = acc[j];
             } else {
-                const int ea = a.ea[m];
-                const int base_ex = ea - 2056 - 7 * (S - 1) + a.R;
+                const int base_ex = a.ea[m] - 2056 - 7 * (S - 1) + a.R;
 #pragma unroll
-                for (int j = 0; j < TN; ++j) {
-                    const int64_t n = tn * TN + j;
-                    if (n < a.N) {
-                        const double v = scale_pow2(acc[j], base_ex + a.eb[n]);
-                        a.out.p[out_addr(a.out, m, n)] = v;
-                    }
+                for (int j = 0; j < HC; ++j) {
+                    const int64_t n = n0 + j;
+                    if (n < a.N) a.out.p[out_addr(a.out, m, n)] = scale_pow2(acc[j], base_ex + a.eb[n]);
                 }
             }
         }
@@ -553,7 +589,7 @@ rt_status slice_operand(const Operand& op, int64_t K, int T, Sliced& out, cudaSt
         const int64_t warps = std::min<int64_t>(op.rows, 64ll * sm_count());
         emax_contig_kernel<<<(unsigned)ceil_div(warps * 32, 256), 256, 0, stream>>>(op, K, out.emax.as<int>(), err);
         RT_TRY(check_launch("emax_contig_kernel"));
-        dim3 grid((unsigned)out.tiles, (unsigned)out.Kb);
+        dim3 grid((unsigned)out.tiles, (unsigned)ceil_div(K, SK));
         slice_contig_kernel<S><<<grid, 256, 0, stream>>>(sa);
         RT_TRY(check_launch("slice_contig_kernel"));
     } else if (op.s0 == 1) {
@@ -562,7 +598,7 @@ rt_status slice_operand(const Operand& op, int64_t K, int T, Sliced& out, cudaSt
         dim3 g1((unsigned)ceil_div(op.rows, 256), (unsigned)ceil_div(K, kspan));
         emax_strided_kernel<<<g1, 256, 0, stream>>>(op, K, kspan, out.emax.as<int>(), err);
         RT_TRY(check_launch("emax_strided_kernel"));
-        dim3 grid((unsigned)out.tiles, (unsigned)out.Kb);
+        dim3 grid((unsigned)out.tiles, (unsigned)ceil_div(K, SK));
         slice_strided_kernel<S><<<grid, 256, 0, stream>>>(sa);
         RT_TRY(check_launch("slice_strided_kernel"));
     } else {
@@ -616,7 +652,7 @@ rt_status run(const OzGemm& g, cudaStream_t stream) {
     a.Kb = sa.Kb;
     a.tiles_m = ceil_div(a.M, TM);
     a.tiles_n = ceil_div(a.N, TN);
-    a.chunk_kb = chunk_kblocks(S);
+    a.chunk_kb = (int)balanced_chunk_kb(a.Kb, S);
     a.nchunks = ceil_div(a.Kb, a.chunk_kb);
     a.symmetric = g.symmetric;
     a.out = OutMap{g.C.p, g.C.md, g.C.ms0, g.C.ms1, g.C.nd, g.C.ns0, g.C.ns1};
@@ -661,7 +697,7 @@ rt_status run(const OzGemm& g, cudaStream_t stream) {
         a.partial = part.as<int64_t>();
     }
     constexpr int smem = num_stages(S) * stage_bytes(S) + 256;
-    dim3 grid((unsigned)tiles, (unsigned)splits);
+    dim3 grid((unsigned)std::min<int64_t>(tiles * splits, sms));
     // Algorithmic tensor work: S(S+1)/2 digit-pair products of 2*M*N*K each
     // (half of the square for the symmetric product).
     const double pair_flops = 2.0 * (double)a.M * (double)a.N * (double)g.K * (g.symmetric ? 0.5 : 1.0);
