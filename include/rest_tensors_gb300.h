@@ -144,6 +144,52 @@ rt_status rt_ri_j(const double* B, const double* D, int nb, int naux, double* w,
  * float64 with a fixed-order tree.  Writes one double to ex_device. */
 rt_status rt_ri_exchange_energy(const double* D, const double* K, int nb, double* ex_device, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Response operator and Davidson solver.
+ * ------------------------------------------------------------------------ */
+
+/* (ia|jb) block M = B_ov B_ov^T, B_ov = [nov, naux] column-major (the (i,a,P)
+ * output of rt_ri_ov_k viewed as [nocc*nvir, naux]); M = [nov, nov]. */
+rt_status rt_ri_iajb(const double* Bov, long long nov, int naux, double* M, int form, int nslices, void* stream);
+
+/* RI response operator on a block of vectors, A = diag(delta) + B_ov B_ov^T:
+ * AX = delta .* X + B_ov (B_ov^T X), X and AX = [nov, nvec]. */
+rt_status rt_ri_response_matvec(const double* Bov, const double* delta, long long nov, int naux, const double* X,
+                                double* AX, int nvec, int form, int nslices, void* stream);
+
+/* Matrix-vector product callback for the Davidson solver: ax[:, v] = A x[:, v]
+ * for the nvec columns of x (device pointers, column-major, leading dimension
+ * n), on `stream`.  It plays the role of the `a_x` closure of
+ * davidson_solve (src/davidson.rs:48-53). */
+typedef rt_status (*rt_matvec_fn)(const double* x, double* ax, int nvec, long long n, void* ctx, void* stream);
+
+/* DavidsonParams (src/davidson.rs:28-46); defaults tol 1e-5, maxcyc 50,
+ * maxspace 12, lindep 1e-14, nroots 3. */
+typedef struct {
+    double tol;
+    int maxcyc;
+    int maxspace;
+    double lindep;
+    int nroots;
+} rt_davidson_params;
+
+/* Lowest `nroots` eigenpairs of a symmetric operator, davidson_solve
+ * (src/davidson.rs:48-266): one starting vector x0_1d, diagonal hdiag for the
+ * preconditioner (both device, length n).  Outputs conv[nroots], e[nroots]
+ * (host) and x_out[n, nroots] (device); `iterations` receives the cycle count
+ * (may be NULL).  Vectors stay on the device; the subspace eigenproblem is
+ * solved in float64 on the host. */
+rt_status rt_davidson_solve(rt_matvec_fn a_x, void* ctx, const double* x0_1d, const double* hdiag, long long n,
+                            const rt_davidson_params* params, int print_level, int* conv, double* e, double* x_out,
+                            int* iterations, void* stream);
+
+/* rt_davidson_solve on the RI response operator diag(delta) + B_ov B_ov^T.
+ * The preconditioner uses the operator's exact diagonal,
+ * delta[ia] + sum_P B_ov[ia, P]^2, formed on the device. */
+rt_status rt_davidson_ri_response(const double* Bov, const double* delta, long long nov, int naux, int form,
+                                  int nslices, const double* x0_1d, const rt_davidson_params* params, int print_level,
+                                  int* conv, double* e, double* x_out, int* iterations, void* stream);
+
 /* Fill B[nb, nb, naux] with the deterministic synthetic ri3ao tensor of
  * include/rt_synth.h (slabs P0..P0+nslab-1 of the full tensor, stored from B). */
 rt_status rt_synth_ri3ao(uint64_t seed, int nb, int P0, int nslab, double* B, void* stream);

@@ -37,6 +37,15 @@ _lib = None
 _dp = ctypes.POINTER(ctypes.c_double)
 
 
+class _DavidsonParamsC(ctypes.Structure):
+    _fields_ = [("tol", ctypes.c_double), ("maxcyc", ctypes.c_int), ("maxspace", ctypes.c_int),
+                ("lindep", ctypes.c_double), ("nroots", ctypes.c_int)]
+
+
+MATVEC_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong,
+                             ctypes.c_void_p, ctypes.c_void_p)
+
+
 class RTError(RuntimeError):
     """A non-zero rt_status from the native library."""
 
@@ -89,6 +98,17 @@ def lib() -> ctypes.CDLL:
     L.rt_profile_get.restype = c_int
     L.rt_profile_get.argtypes = [c_int, ctypes.POINTER(c_dbl), ctypes.POINTER(ctypes.c_longlong),
                                  ctypes.POINTER(c_dbl)]
+    L.rt_ri_iajb.restype = c_int
+    L.rt_ri_iajb.argtypes = [vp, ctypes.c_longlong, c_int, vp, c_int, c_int, vp]
+    L.rt_ri_response_matvec.restype = c_int
+    L.rt_ri_response_matvec.argtypes = [vp, vp, ctypes.c_longlong, c_int, vp, vp, c_int, c_int, c_int, vp]
+    L.rt_davidson_solve.restype = c_int
+    L.rt_davidson_solve.argtypes = [MATVEC_FN, vp, vp, vp, ctypes.c_longlong, ctypes.POINTER(_DavidsonParamsC), c_int,
+                                    ctypes.POINTER(c_int), ctypes.POINTER(c_dbl), vp, ctypes.POINTER(c_int), vp]
+    L.rt_davidson_ri_response.restype = c_int
+    L.rt_davidson_ri_response.argtypes = [vp, vp, ctypes.c_longlong, c_int, c_int, c_int, vp,
+                                          ctypes.POINTER(_DavidsonParamsC), c_int, ctypes.POINTER(c_int),
+                                          ctypes.POINTER(c_dbl), vp, ctypes.POINTER(c_int), vp]
     L.ri_ao2mo_f_.restype = None
     L.general_dgemm_f_.restype = None
     _lib = L
@@ -241,6 +261,8 @@ def _dptr(t) -> int:
 
     if t is None:
         return None
+    if isinstance(t, int):
+        return t
     if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float64 and t.is_contiguous()):
         raise TypeError("expected a contiguous float64 CUDA tensor")
     return t.data_ptr()
@@ -367,6 +389,104 @@ def profile_get(kind: int):
     ms, n, w = ctypes.c_double(), ctypes.c_longlong(), ctypes.c_double()
     _check(lib().rt_profile_get(kind, ctypes.byref(ms), ctypes.byref(n), ctypes.byref(w)))
     return ms.value, n.value, w.value
+
+
+# --------------------------------------------------------------------------
+# Response operator and Davidson
+# --------------------------------------------------------------------------
+class DavidsonParams:
+    """DavidsonParams (src/davidson.rs:28-46), same field names and defaults."""
+
+    def __init__(self, tol=1e-5, maxcyc=50, maxspace=12, lindep=1e-14, nroots=3):
+        self.tol, self.maxcyc, self.maxspace, self.lindep, self.nroots = tol, maxcyc, maxspace, lindep, nroots
+
+    def _c(self):
+        return _DavidsonParamsC(self.tol, self.maxcyc, self.maxspace, self.lindep, self.nroots)
+
+
+def _device_view(ptr: int, nvec: int, n: int):
+    """A torch view [nvec, n] of a column-major device block [n, nvec]."""
+    import torch
+
+    class _Arr:
+        pass
+
+    o = _Arr()
+    o.__cuda_array_interface__ = {"shape": (nvec, n), "typestr": "<f8", "data": (int(ptr), False), "version": 3,
+                                  "strides": None}
+    return torch.as_tensor(o, device="cuda")
+
+
+def ri_iajb(Bov, nov: int, naux: int, M=None, form: str = "split", nslices: int = DEFAULT_NSLICES, stream=None):
+    import torch
+
+    if M is None:
+        M = torch.empty(nov * nov, dtype=torch.float64, device=Bov.device)
+    _check(lib().rt_ri_iajb(_dptr(Bov), nov, naux, _dptr(M), _form(form), nslices, _stream(stream)))
+    return M
+
+
+def ri_response_matvec(Bov, delta, nov: int, naux: int, X, nvec: int, AX=None, form: str = "split",
+                       nslices: int = DEFAULT_NSLICES, stream=None):
+    import torch
+
+    if AX is None:
+        AX = torch.empty(nov * nvec, dtype=torch.float64, device=Bov.device)
+    _check(lib().rt_ri_response_matvec(_dptr(Bov), _dptr(delta), nov, naux, _dptr(X), _dptr(AX), nvec, _form(form),
+                                       nslices, _stream(stream)))
+    return AX
+
+
+def davidson_solve(a_x, x0_1d, hdiag, params: DavidsonParams = None, print_level: int = 0, stream=None):
+    """davidson_solve (src/davidson.rs:48-266) with vectors on the device.
+
+    a_x(X) receives a torch view [nvec, n] (row v = vector v) and returns A X in
+    the same shape; it plays the role of the reference's `a_x` closure.
+    Returns (conv: list[bool], e: list[float], x: torch [nroots, n]).
+    """
+    import torch
+
+    params = params or DavidsonParams()
+    n = int(x0_1d.numel())
+
+    def cb(xp, axp, nvec, nn, ctx, st):
+        try:
+            X = _device_view(xp, nvec, nn)
+            AX = _device_view(axp, nvec, nn)
+            AX.copy_(a_x(X))
+            return 0
+        except Exception as ex:  # reported to the native side as a failed callback
+            print("davidson a_x callback failed:", ex)
+            return 1
+
+    cfn = MATVEC_FN(cb)
+    nr = params.nroots
+    conv = (ctypes.c_int * nr)()
+    e = (ctypes.c_double * nr)()
+    its = ctypes.c_int(0)
+    x = torch.zeros(nr * n, dtype=torch.float64, device=x0_1d.device)
+    pc = params._c()
+    _check(lib().rt_davidson_solve(cfn, None, _dptr(x0_1d), _dptr(hdiag), n, ctypes.byref(pc), print_level, conv, e,
+                                   _dptr(x), ctypes.byref(its), _stream(stream)))
+    return [bool(c) for c in conv], list(e), x.view(nr, n), its.value
+
+
+def davidson_ri_response(Bov, delta, nov: int, naux: int, x0_1d, params: DavidsonParams = None, form: str = "split",
+                         nslices: int = DEFAULT_NSLICES, print_level: int = 0, stream=None):
+    """Lowest roots of diag(delta) + B_ov B_ov^T by the native Davidson driver."""
+    import torch
+
+    params = params or DavidsonParams()
+    nr = params.nroots
+    conv = (ctypes.c_int * nr)()
+    e = (ctypes.c_double * nr)()
+    its = ctypes.c_int(0)
+    x = torch.zeros(nr * nov, dtype=torch.float64, device=Bov.device)
+    pc = params._c()
+    _check(lib().rt_davidson_ri_response(_dptr(Bov), _dptr(delta), nov, naux, _form(form), nslices, _dptr(x0_1d),
+                                         ctypes.byref(pc), print_level, conv, e, _dptr(x), ctypes.byref(its),
+                                         _stream(stream)))
+    return [bool(c) for c in conv], list(e), x.view(nr, nov), its.value
 
 
 def sync_status(stream=None) -> None:

@@ -27,6 +27,8 @@ def declared_functions():
         text = re.sub(r"\{[^{}]*\}", ";", text)
         for stmt in text.split(";"):
             stmt = " ".join(stmt.split())
+            if stmt.startswith("typedef"):
+                continue
             m = re.match(r"^(?:extern \"C\" )?[A-Za-z_][\w\s\*]*?\b([A-Za-z_]\w*)\s*\(.*\)$", stmt)
             if m and not re.search(r"\b(static|inline|RT_SYNTH_FN)\b", stmt):
                 names.add(m.group(1))
