@@ -4,6 +4,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <vector>
 
 #include "rt_internal.cuh"
 
@@ -58,6 +59,74 @@ rt_status ri_ao2mo_split(const double* C, const double* B, double* R, int nb, in
     return RT_OK;
 }
 
+// Half-transform and ov block for slabs [P0, P0 + np) of B (B already offset to slab P0):
+//   X^P = B^P C_occ  ->  X[mu + nb i + nb nocc P],   ov[i,a,P] = (X^P^T C_vir)[i,a].
+rt_status ri_ov_block(const double* C, const double* B, int nb, int64_t np, int nocc, int nvir, double* X,
+                      double* ov, int form, int S, cudaStream_t stream) {
+    const int64_t per = (int64_t)nb * nocc;
+    if (form == RT_FORM_FP64) {
+        GemmF64 g1;
+        g1.opa = 'N'; g1.opb = 'N'; g1.m = nb; g1.n = nocc; g1.k = nb;
+        g1.A = B; g1.lda = nb; g1.sA = (int64_t)nb * nb;
+        g1.B = C; g1.ldb = nb; g1.sB = 0;
+        g1.C = X; g1.rsC = 1; g1.csC = nb; g1.bsC = per; g1.batch = np;
+        RT_TRY(gemm_f64(g1, stream));
+        if (ov && nvir > 0) {
+            GemmF64 g2;
+            g2.opa = 'T'; g2.opb = 'N'; g2.m = nocc; g2.n = nvir; g2.k = nb;
+            g2.A = X; g2.lda = nb; g2.sA = per;
+            g2.B = C + per; g2.ldb = nb; g2.sB = 0;
+            g2.C = ov; g2.rsC = 1; g2.csC = nocc; g2.bsC = (int64_t)nocc * nvir; g2.batch = np;
+            RT_TRY(gemm_f64(g2, stream));
+        }
+        return RT_OK;
+    }
+    // A(m=(mu,P), k=nu) = B[mu + nb nu + nb^2 P], B(n=i, k=nu) = C[nu + nb i]
+    OzGemm g1;
+    g1.K = nb;
+    g1.A.p = B; g1.A.rows = (int64_t)nb * np; g1.A.div = nb;
+    g1.A.s0 = 1; g1.A.s1 = (int64_t)nb * nb; g1.A.sk = nb;
+    g1.B.p = C; g1.B.rows = nocc; g1.B.s0 = nb; g1.B.sk = 1;
+    g1.C.p = X; g1.C.md = nb; g1.C.ms0 = 1; g1.C.ms1 = per; g1.C.ns0 = nb;
+    g1.nslices = S;
+    RT_TRY(oz_gemm(g1, stream));
+    if (ov && nvir > 0) {
+        // A(m=(i,P), k=mu) = X[mu + nb m], B(n=a, k=mu) = C_vir[mu + nb a]
+        OzGemm g2;
+        g2.K = nb;
+        g2.A.p = X; g2.A.rows = (int64_t)nocc * np; g2.A.s0 = nb; g2.A.sk = 1;
+        g2.B.p = C + per; g2.B.rows = nvir; g2.B.s0 = nb; g2.B.sk = 1;
+        g2.C.p = ov; g2.C.md = nocc; g2.C.ms0 = 1; g2.C.ms1 = (int64_t)nocc * nvir; g2.C.ns0 = nocc;
+        g2.nslices = S;
+        RT_TRY(oz_gemm(g2, stream));
+    }
+    return RT_OK;
+}
+
+// K[mu,nu] = sum_{(i,P)} X[mu + nb k] X[nu + nb k], k = i + nocc P.
+rt_status ri_k_from_x(const double* X, int nb, int nocc, int naux, double* K, int form, int S, cudaStream_t stream) {
+    const int64_t kdim = (int64_t)nocc * naux;
+    if (form == RT_FORM_FP64) {
+        GemmF64 g3;
+        g3.opa = 'N'; g3.opb = 'T'; g3.m = nb; g3.n = nb; g3.k = kdim;
+        g3.A = X; g3.lda = nb; g3.B = X; g3.ldb = nb;
+        g3.C = K; g3.rsC = 1; g3.csC = nb;
+        const int64_t tiles = ceil_div(nb, 64) * ceil_div(nb, 64);
+        const int64_t want = (4 * sm_count() + tiles - 1) / tiles;
+        g3.splitk = (int)std::max<int64_t>(1, std::min<int64_t>(want, kdim / 256));
+        return gemm_f64(g3, stream);
+    }
+    OzGemm g3;
+    g3.K = kdim;
+    g3.A.p = X; g3.A.rows = nb; g3.A.s0 = 1; g3.A.sk = nb;
+    g3.B = g3.A;
+    g3.b_is_a = true;
+    g3.symmetric = true;
+    g3.C.p = K; g3.C.ms0 = 1; g3.C.ns0 = nb;
+    g3.nslices = S;
+    return oz_gemm(g3, stream);
+}
+
 rt_status ri_ov_k_split(const double* C, const double* B, int nb, int naux, int nocc, int nvir, double* ov,
                         double* K, int S, cudaStream_t stream) {
     const int64_t per = (int64_t)nb * nocc;
@@ -67,39 +136,10 @@ rt_status ri_ov_k_split(const double* C, const double* B, int nb, int naux, int 
     const int64_t blk = split_block(nb, naux, S);
     for (int64_t P0 = 0; P0 < naux; P0 += blk) {
         const int64_t np = std::min<int64_t>(blk, naux - P0);
-        // X^P = B^P C_occ, stored X[mu + nb i + nb nocc P]
-        OzGemm g1;
-        g1.K = nb;
-        g1.A.p = B + P0 * (int64_t)nb * nb; g1.A.rows = (int64_t)nb * np; g1.A.div = nb;
-        g1.A.s0 = 1; g1.A.s1 = (int64_t)nb * nb; g1.A.sk = nb;
-        g1.B.p = C; g1.B.rows = nocc; g1.B.s0 = nb; g1.B.sk = 1;
-        g1.C.p = X + P0 * per; g1.C.md = nb; g1.C.ms0 = 1; g1.C.ms1 = per; g1.C.ns0 = nb;
-        g1.nslices = S;
-        RT_TRY(oz_gemm(g1, stream));
-        if (ov && nvir > 0) {
-            // ov[i,a,P] = sum_mu X^P[mu,i] C_vir[mu,a]: A(m=(i,P), k=mu) = X[mu + nb m]
-            OzGemm g2;
-            g2.K = nb;
-            g2.A.p = X + P0 * per; g2.A.rows = (int64_t)nocc * np; g2.A.s0 = nb; g2.A.sk = 1;
-            g2.B.p = C + per; g2.B.rows = nvir; g2.B.s0 = nb; g2.B.sk = 1;
-            g2.C.p = ov + P0 * (int64_t)nocc * nvir; g2.C.md = nocc; g2.C.ms0 = 1;
-            g2.C.ms1 = (int64_t)nocc * nvir; g2.C.ns0 = nocc;
-            g2.nslices = S;
-            RT_TRY(oz_gemm(g2, stream));
-        }
+        RT_TRY(ri_ov_block(C, B + P0 * (int64_t)nb * nb, nb, np, nocc, nvir, X + P0 * per,
+                           ov ? ov + P0 * (int64_t)nocc * nvir : nullptr, RT_FORM_SPLIT, S, stream));
     }
-    if (K) {
-        // K[mu,nu] = sum_{(i,P)} X[mu + nb k] X[nu + nb k], k = i + nocc P
-        OzGemm g3;
-        g3.K = (int64_t)nocc * naux;
-        g3.A.p = X; g3.A.rows = nb; g3.A.s0 = 1; g3.A.sk = nb;
-        g3.B = g3.A;
-        g3.b_is_a = true;
-        g3.symmetric = true;
-        g3.C.p = K; g3.C.ms0 = 1; g3.C.ns0 = nb;
-        g3.nslices = S;
-        RT_TRY(oz_gemm(g3, stream));
-    }
+    if (K) RT_TRY(ri_k_from_x(X, nb, nocc, naux, K, RT_FORM_SPLIT, S, stream));
     return RT_OK;
 }
 
@@ -228,18 +268,87 @@ rt_status rt_ri_ov_k_host(const double* C, const double* B, int nb, int naux, in
     cudaStream_t s = (cudaStream_t)stream;
     const size_t nC = (size_t)nb * (nocc + nvir), nB = (size_t)nb * nb * naux;
     const size_t nO = (size_t)nocc * nvir * naux, nK = (size_t)nb * nb;
-    ScratchBuf dC, dB, dO, dK;
-    RT_TRY(scratch_alloc(dC, sizeof(double) * std::max<size_t>(nC, 1), s));
-    RT_TRY(scratch_alloc(dB, sizeof(double) * std::max<size_t>(nB, 1), s));
-    if (ov) RT_TRY(scratch_alloc(dO, sizeof(double) * std::max<size_t>(nO, 1), s));
-    if (K) RT_TRY(scratch_alloc(dK, sizeof(double) * std::max<size_t>(nK, 1), s));
-    if (nC) RT_CUDA_TRY(cudaMemcpyAsync(dC.p, C, sizeof(double) * nC, cudaMemcpyHostToDevice, s));
-    if (nB) RT_CUDA_TRY(cudaMemcpyAsync(dB.p, B, sizeof(double) * nB, cudaMemcpyHostToDevice, s));
+    const int64_t per = (int64_t)nb * nocc, slab = (int64_t)nb * nb, oslab = (int64_t)nocc * nvir;
+    if (nB == 0 || nocc == 0) {
+        if (ov && nO) memset(ov, 0, sizeof(double) * nO);
+        if (K && nK) memset(K, 0, sizeof(double) * nK);
+        return RT_OK;
+    }
+    ScratchBuf dC, dB, dX, dO, dK;
+    RT_TRY(scratch_alloc(dC, sizeof(double) * nC, s));
+    RT_TRY(scratch_alloc(dB, sizeof(double) * nB, s));
+    RT_TRY(scratch_alloc(dX, sizeof(double) * (size_t)per * naux, s));
+    if (ov && nO) RT_TRY(scratch_alloc(dO, sizeof(double) * nO, s));
+    if (K) RT_TRY(scratch_alloc(dK, sizeof(double) * nK, s));
     RT_TRY(error_word_reset(s));
-    RT_TRY(rt_ri_ov_k(dC.as<double>(), dB.as<double>(), nb, naux, nocc, nvir, ov ? dO.as<double>() : nullptr,
-                      K ? dK.as<double>() : nullptr, form, nslices, stream));
-    if (ov && nO) RT_CUDA_TRY(cudaMemcpyAsync(ov, dO.p, sizeof(double) * nO, cudaMemcpyDeviceToHost, s));
-    if (K && nK) RT_CUDA_TRY(cudaMemcpyAsync(K, dK.p, sizeof(double) * nK, cudaMemcpyDeviceToHost, s));
+
+    // Slab blocks of ~512 MB: host-to-device copies of block b+1 run on their own
+    // stream while block b is transformed; ov blocks go back on a third stream.
+    const int64_t blk = std::max<int64_t>(1, std::min<int64_t>(naux, ((int64_t)64 << 20) / std::max<int64_t>(slab, 1)));
+    const int64_t nblk = ceil_div(naux, blk);
+    cudaStream_t hs = nullptr, ds = nullptr;
+    cudaEvent_t ready = nullptr;
+    std::vector<cudaEvent_t> in(nblk, nullptr), out(nblk, nullptr);
+    rt_status st = RT_OK;
+    auto fail = [&](cudaError_t e, const char* what) {
+        set_error(RT_ERR_CUDA, "rt_ri_ov_k_host: %s: %s", what, cudaGetErrorString(e));
+        st = RT_ERR_CUDA;
+    };
+    cudaError_t e;
+    if ((e = cudaStreamCreateWithFlags(&hs, cudaStreamNonBlocking)) != cudaSuccess) fail(e, "stream");
+    if (st == RT_OK && (e = cudaStreamCreateWithFlags(&ds, cudaStreamNonBlocking)) != cudaSuccess) fail(e, "stream");
+    if (st == RT_OK && (e = cudaEventCreateWithFlags(&ready, cudaEventDisableTiming)) != cudaSuccess) fail(e, "event");
+    for (int64_t b = 0; st == RT_OK && b < nblk; ++b) {
+        if ((e = cudaEventCreateWithFlags(&in[b], cudaEventDisableTiming)) != cudaSuccess) fail(e, "event");
+        else if ((e = cudaEventCreateWithFlags(&out[b], cudaEventDisableTiming)) != cudaSuccess) fail(e, "event");
+    }
+    if (st == RT_OK) {
+        // The pool allocations above are ordered on `s`; the copy streams start after them.
+        cudaMemcpyAsync(dC.p, C, sizeof(double) * nC, cudaMemcpyHostToDevice, s);
+        cudaEventRecord(ready, s);
+        cudaStreamWaitEvent(hs, ready, 0);
+        cudaStreamWaitEvent(ds, ready, 0);
+        auto compute = [&](int64_t b) -> rt_status {
+            const int64_t P0 = b * blk, np = std::min<int64_t>(blk, naux - P0);
+            cudaStreamWaitEvent(s, in[b], 0);
+            RT_TRY(ri_ov_block(dC.as<double>(), dB.as<double>() + P0 * slab, nb, np, nocc, nvir,
+                               dX.as<double>() + P0 * per, (ov && nO) ? dO.as<double>() + P0 * oslab : nullptr, form,
+                               nslices, s));
+            if (ov && nO) {
+                cudaEventRecord(out[b], s);
+                cudaStreamWaitEvent(ds, out[b], 0);
+                RT_CUDA_TRY(cudaMemcpyAsync(ov + P0 * oslab, dO.as<double>() + P0 * oslab,
+                                            sizeof(double) * (size_t)(np * oslab), cudaMemcpyDeviceToHost, ds));
+            }
+            return RT_OK;
+        };
+        for (int64_t b = 0; st == RT_OK && b < nblk; ++b) {
+            const int64_t P0 = b * blk, np = std::min<int64_t>(blk, naux - P0);
+            if ((e = cudaMemcpyAsync(dB.as<double>() + P0 * slab, B + P0 * slab, sizeof(double) * (size_t)(np * slab),
+                                     cudaMemcpyHostToDevice, hs)) != cudaSuccess) {
+                fail(e, "host-to-device copy");
+                break;
+            }
+            cudaEventRecord(in[b], hs);
+            if (b > 0) st = compute(b - 1);
+        }
+        if (st == RT_OK) st = compute(nblk - 1);
+        if (st == RT_OK && K) {
+            st = ri_k_from_x(dX.as<double>(), nb, nocc, naux, dK.as<double>(), form, nslices, s);
+            if (st == RT_OK && (e = cudaMemcpyAsync(K, dK.p, sizeof(double) * nK, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+                fail(e, "device-to-host copy");
+        }
+    }
+    // Drain both copy streams before the scratch is released on `s`.
+    if (hs) cudaStreamSynchronize(hs);
+    if (ds) cudaStreamSynchronize(ds);
+    cudaStreamSynchronize(s);
+    for (auto ev : in) if (ev) cudaEventDestroy(ev);
+    for (auto ev : out) if (ev) cudaEventDestroy(ev);
+    if (ready) cudaEventDestroy(ready);
+    if (hs) cudaStreamDestroy(hs);
+    if (ds) cudaStreamDestroy(ds);
+    if (st != RT_OK) return st;
     return error_word_check(s, "rt_ri_ov_k_host");
 }
 

@@ -260,3 +260,22 @@ def test_split_rounding_has_no_bias_on_ties():
     exact = [sum(int(j) * int(j) for j in J[i].tolist()) for i in range(nb)]
     rel = np.array([(d[i] * 2.0 ** 96 - exact[i]) / exact[i] for i in range(nb)])
     assert abs(rel.mean()) < 2e-15 and np.max(np.abs(rel)) < 1e-13
+
+
+@pytest.mark.parametrize("form", ["fp64", "split"])
+def test_pipelined_host_entry_is_bitwise_equal_to_device_entry(form):
+    # 864 MB of ri3ao: the host entry streams it in two slab blocks, overlapping
+    # copies with compute; every element's arithmetic is unchanged by blocking.
+    nb, naux, nocc = 600, 300, 60
+    nvir = nb - nocc
+    B = rt.synth_ri3ao(11, nb, naux)
+    C = rt.synth_coef(11, nb)
+    ov, K = rt.ri_ov_k(C, B, nb, naux, nocc, nvir, form=form, nslices=7)
+    hB = torch.empty(B.numel(), dtype=torch.float64).pin_memory()
+    hB.copy_(B)
+    hC = C.cpu()
+    hO = np.zeros(nocc * nvir * naux)
+    hK = np.zeros(nb * nb)
+    rt.ri_ov_k_host(hC.data_ptr(), hB.data_ptr(), nb, naux, nocc, nvir, hO, hK, form=form, nslices=7)
+    assert np.array_equal(hO, ov.cpu().numpy())
+    assert np.array_equal(hK, K.cpu().numpy())
