@@ -58,6 +58,8 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--sweep", default="", help="comma list of slice counts to also report (time, errors)")
     p.add_argument("--naux", type=int, default=NAUX, help="auxiliary slabs (smaller values only for profiling runs)")
+    p.add_argument("--batch-mols", type=int, default=64, help="molecules of the batched uneven-size leg (0: skip)")
+    p.add_argument("--batch-steps", type=int, default=20)
     return p.parse_args()
 
 
@@ -110,6 +112,77 @@ class ClockSampler:
         reasons = sorted({names[i] for _, _, r in rows for i in range(4) if r[i].lower().startswith("active")})
         return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
                 "reasons": reasons, "samples": len(rows)}
+
+
+# ------------------------------------------------------------ batched leg --
+def batch_shapes(seed: int, n: int):
+    """n molecules: nbas uniform in [40, 400], naux = 4 nbas, nocc = round(nbas / 10)."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    out = []
+    for nb in rng.integers(40, 401, size=n):
+        nb = int(nb)
+        out.append((nb, 4 * nb, int(round(nb / 10))))
+    return out
+
+
+def batched_leg(args, rt, torch, stream):
+    """Many molecules of uneven size, one grouped launch per product, replayed from a CUDA graph."""
+    from rest_tensors_gb300 import autotune
+
+    shapes = batch_shapes(args.seed, args.batch_mols)
+    probs, flops = [], 0.0
+    for k, (nb, naux, nocc) in enumerate(shapes):
+        nvir = nb - nocc
+        probs.append(dict(C=rt.synth_coef(k, nb), B=rt.synth_ri3ao(k, nb, naux), nb=nb, naux=naux, nocc=nocc,
+                          nvir=nvir,
+                          ov=torch.empty(nocc * nvir * naux, dtype=torch.float64, device="cuda"),
+                          K=torch.empty(nb * nb, dtype=torch.float64, device="cuda")))
+        flops += naux * (4.0 * nb * nb * nocc + 2.0 * nb * nocc * nvir)
+    S = args.nslices
+    out = {"workload": f"{len(shapes)} molecules, nbas uniform in [40, 400] (seed {args.seed}), naux = 4 nbas, "
+                       f"nocc = round(nbas/10); ov transform + RI-K per molecule",
+           "molecules": len(shapes), "flop_per_step": flops,
+           "ri3ao_gb": sum(nb * nb * naux for nb, naux, _ in shapes) * 8 / 1e9,
+           "graph": "one CUDA graph per form, captured once and replayed each step"}
+    res = {}
+    for form in ("fp64", "split"):
+        tuning = autotune.lookup(probs, form, S, stream=stream) if form == "split" else None
+        rt.ri_ov_k_batched(probs, form=form, nslices=S, tuning=tuning, stream=stream)
+        rt.sync_status()
+        if form == "fp64":
+            ref = [(q["ov"].clone(), q["K"].clone()) for q in probs]
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            rt.ri_ov_k_batched(probs, form=form, nslices=S, tuning=tuning)
+        steps = max(1, args.batch_steps if form == "split" else max(1, args.batch_steps // 10))
+        for _ in range(3):
+            g.replay()
+        torch.cuda.synchronize()
+        n0 = rt.launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        cs = torch.cuda.current_stream()
+        e0.record(cs)
+        for _ in range(steps):
+            g.replay()
+        e1.record(cs)
+        torch.cuda.synchronize()
+        rt.sync_status()
+        ms = e0.elapsed_time(e1) / steps
+        res[form] = {"tflops": flops / ms / 1e9, "ms_per_step": ms, "steps": steps}
+        if tuning is not None:
+            res[form]["tuning"] = {"fuse": tuning.fuse, "chunks_per_item": tuning.chunks_per_item,
+                                   "table": autotune.table_path()}
+        del g
+    ov_err = max(float((q["ov"] - r[0]).abs().max()) for q, r in zip(probs, ref))
+    k_err = max(float((q["K"] - r[1]).abs().max() / r[1].abs().max()) for q, r in zip(probs, ref))
+    out.update(res)
+    out["speedup_vs_fp64"] = res["fp64"]["ms_per_step"] / res["split"]["ms_per_step"]
+    out["errors_vs_fp64"] = {"ov_max_abs": ov_err, "K_max_rel": k_err}
+    del probs, ref
+    torch.cuda.empty_cache()
+    return out
 
 
 # ------------------------------------------------------------ CPU baseline --
@@ -328,6 +401,12 @@ def main():
                "path": "rt_ri_ov_k_host (C ABI, pinned host buffers, copies inside the timed region)"}
         del hB
 
+    batched = None
+    if args.batch_mols > 0:
+        del ov, K
+        torch.cuda.empty_cache()
+        batched = batched_leg(args, rt, torch, stream)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(args.seed)
@@ -348,6 +427,8 @@ def main():
             "e2e": e2e, "cpu_baseline": cpu}
     if sweep:
         line["sweep"] = sweep
+    if batched:
+        line["batched"] = batched
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

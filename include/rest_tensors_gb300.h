@@ -135,6 +135,34 @@ rt_status rt_ri_ov_k(const double* C, const double* B, int nb, int naux, int noc
 rt_status rt_ri_ov_k_fp64_noalloc(const double* C, const double* B, int nb, int naux, int nocc, int nvir, double* ov,
                                   double* K, void* stream);
 
+/* One molecule of a batch: device pointers and sizes as for rt_ri_ov_k. */
+typedef struct {
+    const double* C;
+    const double* B;
+    double* ov;
+    double* K;
+    int nb, naux, nocc, nvir;
+} rt_ri_problem;
+
+/* Launch options of the split form.  fuse: form the ri3ao digits inside the
+ * GEMM instead of a separate slicing pass (less scratch, usually slower);
+ * chunks_per_item: exact contraction chunks per work item of the persistent
+ * GEMM (split-K granularity), 0 = fill whole waves.  Chosen per batch shape
+ * by the package's autotuner. */
+typedef struct {
+    int fuse;
+    int chunks_per_item;
+} rt_tuning;
+
+/* rt_ri_ov_k for many independent molecules of uneven sizes.  Each of the
+ * three products (X = B C_occ, ov, K) of all molecules goes out as one grouped
+ * persistent GEMM launch (split form, up to 48 molecules per launch) or one
+ * grouped DFMA launch (float64 form, up to 64).  The call makes no host
+ * synchronisation and can be captured in a CUDA graph (after a first,
+ * uncaptured call has set the kernels' shared-memory limits). tuning may be NULL. */
+rt_status rt_ri_ov_k_batched(const rt_ri_problem* probs, int nprob, int form, int nslices, const rt_tuning* tuning,
+                             void* stream);
+
 /* RI-J: w[P] = sum_{mu,nu} B^P[mu,nu] D[mu,nu] ("ip,ip->p", _einsum_02,
  * src/matrix/matrix_blas_lapack.rs:1293-1310 on the [nb*nb, naux] view of
  * ri.rs:309-316) and J = sum_P w[P] B^P.  w may be NULL. */

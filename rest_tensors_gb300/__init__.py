@@ -31,7 +31,7 @@ LIB_PATH = os.path.join(HERE, "librest_tensors_gb300.so")
 RT_OK = 0
 RT_FORM_FP64 = 0
 RT_FORM_SPLIT = 1
-DEFAULT_NSLICES = 6
+DEFAULT_NSLICES = 7
 
 _lib = None
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -44,6 +44,17 @@ class _DavidsonParamsC(ctypes.Structure):
 
 MATVEC_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong,
                              ctypes.c_void_p, ctypes.c_void_p)
+
+
+class RiProblem(ctypes.Structure):
+    """One molecule of a batch (``rt_ri_problem``): device addresses and sizes."""
+    _fields_ = [("C", ctypes.c_void_p), ("B", ctypes.c_void_p), ("ov", ctypes.c_void_p), ("K", ctypes.c_void_p),
+                ("nb", ctypes.c_int), ("naux", ctypes.c_int), ("nocc", ctypes.c_int), ("nvir", ctypes.c_int)]
+
+
+class Tuning(ctypes.Structure):
+    """Launch options of the split form (``rt_tuning``)."""
+    _fields_ = [("fuse", ctypes.c_int), ("chunks_per_item", ctypes.c_int)]
 
 
 class RTError(RuntimeError):
@@ -82,6 +93,8 @@ def lib() -> ctypes.CDLL:
     L.rt_ri_ao2mo.argtypes = [vp, vp, vp, c_int, c_int, c_int, c_int, c_int, vp]
     L.rt_ri_ov_k.restype = c_int
     L.rt_ri_ov_k.argtypes = [vp, vp, c_int, c_int, c_int, c_int, vp, vp, c_int, c_int, vp]
+    L.rt_ri_ov_k_batched.restype = c_int
+    L.rt_ri_ov_k_batched.argtypes = [ctypes.POINTER(RiProblem), c_int, c_int, c_int, ctypes.POINTER(Tuning), vp]
     L.rt_ri_ov_k_host.restype = c_int
     L.rt_ri_ov_k_host.argtypes = [vp, vp, c_int, c_int, c_int, c_int, vp, vp, c_int, c_int, vp]
     L.rt_ri_j.restype = c_int
@@ -317,6 +330,28 @@ def ri_ov_k(C, B, nb: int, naux: int, nocc: int, nvir: int, ov=None, K=None, for
     _check(lib().rt_ri_ov_k(_dptr(C), _dptr(B), nb, naux, nocc, nvir, _dptr(ov) if want_ov else None,
                             _dptr(K) if want_k else None, _form(form), nslices, _stream(stream)))
     return ov, K
+
+
+def ri_ov_k_batched(problems, form: str = "split", nslices: int = DEFAULT_NSLICES, tuning=None, stream=None):
+    """rt_ri_ov_k over a batch of molecules of uneven sizes, one grouped launch per product.
+
+    ``problems`` is a sequence of dicts with keys C, B, ov, K (torch CUDA float64
+    tensors or None for ov/K) and nb, naux, nocc, nvir.  ``tuning`` is a
+    ``Tuning``, a ``(fuse, chunks_per_item)`` pair, ``"auto"`` (look the batch
+    up in the autotuned table, tuning it on a miss) or None (defaults).
+    """
+    arr = (RiProblem * max(len(problems), 1))()
+    for i, q in enumerate(problems):
+        arr[i] = RiProblem(_dptr(q["C"]), _dptr(q["B"]), _dptr(q.get("ov")), _dptr(q.get("K")),
+                           q["nb"], q["naux"], q["nocc"], q["nvir"])
+    if isinstance(tuning, str) and tuning == "auto":
+        from . import autotune
+
+        tuning = autotune.lookup(problems, form, nslices, stream=stream)
+    if tuning is not None and not isinstance(tuning, Tuning):
+        tuning = Tuning(int(tuning[0]), int(tuning[1]))
+    _check(lib().rt_ri_ov_k_batched(arr, len(problems), _form(form), nslices,
+                                    ctypes.byref(tuning) if tuning is not None else None, _stream(stream)))
 
 
 def ri_ov_k_host(C: np.ndarray, B: np.ndarray, nb: int, naux: int, nocc: int, nvir: int, ov: np.ndarray,

@@ -231,6 +231,105 @@ rt_status rt_ri_ov_k(const double* C, const double* B, int nb, int naux, int noc
     return ri_ov_k_split(C, B, nb, naux, nocc, nvir, ov, K, nslices, s);
 }
 
+rt_status rt_ri_ov_k_batched(const rt_ri_problem* probs, int nprob, int form, int nslices, const rt_tuning* tuning,
+                             void* stream) {
+    RT_REQUIRE(nprob >= 0 && (nprob == 0 || probs), "rt_ri_ov_k_batched: bad problem list");
+    RT_REQUIRE(valid_form(form, nslices), "rt_ri_ov_k_batched: bad form/nslices (%d, %d)", form, nslices);
+    cudaStream_t s = (cudaStream_t)stream;
+    size_t xtotal = 0;
+    std::vector<size_t> xoff(nprob);
+    for (int i = 0; i < nprob; ++i) {
+        const rt_ri_problem& q = probs[i];
+        RT_REQUIRE(q.nb >= 0 && q.naux >= 0 && q.nocc >= 0 && q.nvir >= 0,
+                   "rt_ri_ov_k_batched: problem %d has a negative dimension", i);
+        RT_REQUIRE((int64_t)q.nb * q.naux * q.nocc == 0 || (q.C && q.B), "rt_ri_ov_k_batched: problem %d null input", i);
+        xoff[i] = xtotal;
+        xtotal += (size_t)q.nb * q.nocc * q.naux;
+    }
+    ScratchBuf xb;
+    RT_TRY(scratch_alloc(xb, sizeof(double) * std::max<size_t>(xtotal, 1), s));
+    // Problems whose products are empty still get their outputs zeroed.
+    for (int i = 0; i < nprob; ++i) {
+        const rt_ri_problem& q = probs[i];
+        if ((int64_t)q.nocc * q.naux == 0 || q.nb == 0) {
+            if (q.K && q.nb) RT_CUDA_TRY(cudaMemsetAsync(q.K, 0, sizeof(double) * q.nb * (size_t)q.nb, s));
+            if (q.ov && (int64_t)q.nocc * q.nvir * q.naux > 0)
+                RT_CUDA_TRY(cudaMemsetAsync(q.ov, 0, sizeof(double) * (size_t)q.nocc * q.nvir * q.naux, s));
+        }
+    }
+    auto live = [&](const rt_ri_problem& q) { return (int64_t)q.nb * q.naux * q.nocc > 0; };
+    double* X = xb.as<double>();
+    if (form == RT_FORM_FP64) {
+        std::vector<GemmF64> g1, g2, g3;
+        for (int i = 0; i < nprob; ++i) {
+            const rt_ri_problem& q = probs[i];
+            if (!live(q)) continue;
+            const int64_t per = (int64_t)q.nb * q.nocc;
+            GemmF64 a;
+            a.opa = 'N'; a.opb = 'N'; a.m = q.nb; a.n = q.nocc; a.k = q.nb;
+            a.A = q.B; a.lda = q.nb; a.sA = (int64_t)q.nb * q.nb; a.B = q.C; a.ldb = q.nb; a.sB = 0;
+            a.C = X + xoff[i]; a.rsC = 1; a.csC = q.nb; a.bsC = per; a.batch = q.naux;
+            g1.push_back(a);
+            if (q.ov && q.nvir > 0) {
+                GemmF64 b;
+                b.opa = 'T'; b.opb = 'N'; b.m = q.nocc; b.n = q.nvir; b.k = q.nb;
+                b.A = X + xoff[i]; b.lda = q.nb; b.sA = per; b.B = q.C + per; b.ldb = q.nb; b.sB = 0;
+                b.C = q.ov; b.rsC = 1; b.csC = q.nocc; b.bsC = (int64_t)q.nocc * q.nvir; b.batch = q.naux;
+                g2.push_back(b);
+            }
+            if (q.K) {
+                GemmF64 c;
+                c.opa = 'N'; c.opb = 'T'; c.m = q.nb; c.n = q.nb; c.k = per / q.nb * q.naux;
+                c.A = X + xoff[i]; c.lda = q.nb; c.B = X + xoff[i]; c.ldb = q.nb;
+                c.C = q.K; c.rsC = 1; c.csC = q.nb;
+                g3.push_back(c);
+            }
+        }
+        RT_TRY(gemm_f64_many(g1.data(), (int)g1.size(), s));
+        RT_TRY(gemm_f64_many(g2.data(), (int)g2.size(), s));
+        RT_TRY(gemm_f64_many(g3.data(), (int)g3.size(), s));
+        return RT_OK;
+    }
+    const int fuse = tuning ? tuning->fuse : 0;
+    const int cpi = tuning ? tuning->chunks_per_item : 0;
+    std::vector<OzGemm> g1, g2, g3;
+    for (int i = 0; i < nprob; ++i) {
+        const rt_ri_problem& q = probs[i];
+        if (!live(q)) continue;
+        const int64_t per = (int64_t)q.nb * q.nocc;
+        OzGemm a;
+        a.K = q.nb;
+        a.A.p = q.B; a.A.rows = (int64_t)q.nb * q.naux; a.A.div = q.nb; a.A.s0 = 1; a.A.s1 = (int64_t)q.nb * q.nb;
+        a.A.sk = q.nb;
+        a.B.p = q.C; a.B.rows = q.nocc; a.B.s0 = q.nb; a.B.sk = 1;
+        a.C.p = X + xoff[i]; a.C.md = q.nb; a.C.ms0 = 1; a.C.ms1 = per; a.C.ns0 = q.nb;
+        a.nslices = nslices; a.allow_fuse = fuse != 0; a.chunks_per_item = cpi;
+        g1.push_back(a);
+        if (q.ov && q.nvir > 0) {
+            OzGemm b;
+            b.K = q.nb;
+            b.A.p = X + xoff[i]; b.A.rows = (int64_t)q.nocc * q.naux; b.A.s0 = q.nb; b.A.sk = 1;
+            b.B.p = q.C + per; b.B.rows = q.nvir; b.B.s0 = q.nb; b.B.sk = 1;
+            b.C.p = q.ov; b.C.md = q.nocc; b.C.ms0 = 1; b.C.ms1 = (int64_t)q.nocc * q.nvir; b.C.ns0 = q.nocc;
+            b.nslices = nslices; b.chunks_per_item = cpi;
+            g2.push_back(b);
+        }
+        if (q.K) {
+            OzGemm c;
+            c.K = (int64_t)q.nocc * q.naux;
+            c.A.p = X + xoff[i]; c.A.rows = q.nb; c.A.s0 = 1; c.A.sk = q.nb;
+            c.B = c.A; c.b_is_a = true; c.symmetric = true;
+            c.C.p = q.K; c.C.ms0 = 1; c.C.ns0 = q.nb;
+            c.nslices = nslices; c.chunks_per_item = cpi;
+            g3.push_back(c);
+        }
+    }
+    RT_TRY(oz_gemm_many(g1.data(), (int)g1.size(), s));
+    RT_TRY(oz_gemm_many(g2.data(), (int)g2.size(), s));
+    RT_TRY(oz_gemm_many(g3.data(), (int)g3.size(), s));
+    return RT_OK;
+}
+
 rt_status rt_ri_j(const double* B, const double* D, int nb, int naux, double* w, double* J, void* stream) {
     RT_REQUIRE(nb >= 0 && naux >= 0, "rt_ri_j: negative dimension");
     cudaStream_t s = (cudaStream_t)stream;

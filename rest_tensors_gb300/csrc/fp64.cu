@@ -39,19 +39,18 @@ struct GemmArgs {
 // columns ty + 16*j, so a warp reads 16 distinct A values and 2 distinct B
 // values per k step (broadcasts, no bank conflicts).
 template <bool TA, bool TB>
-__global__ void __launch_bounds__(NT) dgemm_tile_kernel(GemmArgs g) {
+__device__ __forceinline__ void dgemm_tile_body(const GemmArgs& g, int64_t tile, int64_t b_first, int64_t b_step,
+                                                int split) {
     __shared__ double As[BK][BM + 1];
     __shared__ double Bs[BK][BN + 1];
     const int tid = threadIdx.x;
     const int tx = tid & 15, ty = tid >> 4;
-    const int64_t tile = blockIdx.x;
     const int64_t tm = tile % g.tiles_m, tn = tile / g.tiles_m;
     const int64_t m0 = tm * BM, n0 = tn * BN;
-    const int split = blockIdx.z;
     const int64_t k0 = (int64_t)split * g.kchunk;
     const int64_t k1 = min(g.k, k0 + g.kchunk);
 
-    for (int64_t b = blockIdx.y; b < g.batch; b += gridDim.y) {
+    for (int64_t b = b_first; b < g.batch; b += b_step) {
         const double* A = g.A + b * g.sA;
         const double* B = g.B + b * g.sB;
         double acc[4][4];
@@ -120,6 +119,31 @@ __global__ void __launch_bounds__(NT) dgemm_tile_kernel(GemmArgs g) {
     }
 }
 
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(NT) dgemm_tile_kernel(GemmArgs g) {
+    dgemm_tile_body<TA, TB>(g, blockIdx.x, blockIdx.y, gridDim.y, blockIdx.z);
+}
+
+// Several float64 GEMMs (same op pair) in one launch: block x enumerates
+// (problem, tile, batch item) through the prefix sums of tiles * batch.
+constexpr int kMaxGroupF64 = 64;
+struct GroupF64 {
+    int n;
+    int64_t prefix[kMaxGroupF64 + 1];
+    GemmArgs a[kMaxGroupF64];
+};
+
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(NT) dgemm_group_kernel(const __grid_constant__ GroupF64 G) {
+    const int64_t blk = blockIdx.x;
+    int p = 0;
+    while (blk >= G.prefix[p + 1]) ++p;
+    const GemmArgs& g = G.a[p];
+    const int64_t local = blk - G.prefix[p];
+    const int64_t tiles = g.tiles_m * g.tiles_n;
+    dgemm_tile_body<TA, TB>(g, local % tiles, local / tiles, g.batch, 0);
+}
+
 // Deterministic split-K reduction: fixed summation order over the splits.
 __global__ void dgemm_splitk_reduce(GemmArgs g) {
     const int64_t mn = g.m * g.n;
@@ -186,6 +210,56 @@ rt_status gemm_f64(const GemmF64& q, cudaStream_t stream) {
     if (splitk > 1) {
         dgemm_splitk_reduce<<<2 * sm_count(), 256, 0, stream>>>(g);
         RT_TRY(check_launch("dgemm_splitk_reduce"));
+    }
+    return RT_OK;
+}
+
+rt_status gemm_f64_many(const GemmF64* qs, int n, cudaStream_t stream) {
+    // Group by op pair; each group goes out in launches of up to kMaxGroupF64 products.
+    for (int op = 0; op < 4; ++op) {
+        const bool ta = op & 1, tb = op & 2;
+        GroupF64 G;
+        G.n = 0;
+        G.prefix[0] = 0;
+        double flops = 0.0;
+        auto flush = [&]() -> rt_status {
+            if (G.n == 0) return RT_OK;
+            for (int i = G.n; i < kMaxGroupF64; ++i) G.prefix[i + 1] = G.prefix[G.n];
+            const int64_t blocks = G.prefix[G.n];
+            if (blocks > 0) {
+                RT_REQUIRE(blocks < (int64_t)INT32_MAX, "gemm_f64_many: too many tiles for one launch");
+                prof_begin(PROF_DGEMM, stream);
+                if (!ta && !tb) dgemm_group_kernel<false, false><<<(unsigned)blocks, NT, 0, stream>>>(G);
+                else if (ta && !tb) dgemm_group_kernel<true, false><<<(unsigned)blocks, NT, 0, stream>>>(G);
+                else if (!ta && tb) dgemm_group_kernel<false, true><<<(unsigned)blocks, NT, 0, stream>>>(G);
+                else dgemm_group_kernel<true, true><<<(unsigned)blocks, NT, 0, stream>>>(G);
+                prof_end(PROF_DGEMM, stream, flops);
+                RT_TRY(check_launch("dgemm_group_kernel"));
+            }
+            G.n = 0;
+            flops = 0.0;
+            return RT_OK;
+        };
+        for (int i = 0; i < n; ++i) {
+            const GemmF64& q = qs[i];
+            if ((q.opa == 'T') != ta || (q.opb == 'T') != tb) continue;
+            RT_REQUIRE(q.m >= 0 && q.n >= 0 && q.k >= 0 && q.batch >= 0, "gemm_f64_many: negative size");
+            if (q.m == 0 || q.n == 0 || q.batch == 0) continue;
+            GemmArgs& g = G.a[G.n];
+            g = GemmArgs{};
+            g.m = q.m; g.n = q.n; g.k = q.k; g.alpha = q.alpha; g.beta = q.beta;
+            g.A = q.A; g.lda = q.lda; g.sA = q.sA; g.B = q.B; g.ldb = q.ldb; g.sB = q.sB;
+            g.C = q.C; g.rsC = q.rsC; g.csC = q.csC; g.bsC = q.bsC; g.batch = q.batch;
+            g.tiles_m = ceil_div(q.m, BM);
+            g.tiles_n = ceil_div(q.n, BN);
+            g.splitk = 1;
+            g.kchunk = std::max<int64_t>(BK, ceil_div(q.k, BK) * BK);
+            G.prefix[G.n + 1] = G.prefix[G.n] + g.tiles_m * g.tiles_n * q.batch;
+            flops += 2.0 * (double)q.m * (double)q.n * (double)q.k * (double)q.batch;
+            ++G.n;
+            if (G.n == kMaxGroupF64) RT_TRY(flush());
+        }
+        RT_TRY(flush());
     }
     return RT_OK;
 }

@@ -35,6 +35,7 @@
 // pipeline stage is a handful of 1-D bulk copies (cp.async.bulk) per operand.
 #include <algorithm>
 #include <cmath>
+#include <vector>
 
 #include "rt_internal.cuh"
 #include "rt_ptx.cuh"
@@ -48,11 +49,18 @@ constexpr int KB = 16;         // k elements per pipeline stage (one MMA k-step)
 constexpr int SK = 32;         // k elements one slicing CTA covers (two k-blocks)
 constexpr int NTHREADS = 320;  // warp 0 producer, warp 1 MMA, warps 2..9 epilogue
 constexpr int EPI_THREADS = 256;
+// Fused variant: warps 10..13 turn float64 tiles staged in shared memory into
+// the A digit planes.
+constexpr int NTHREADS_FUSED = 448;
+constexpr int CONV_THREADS = 128;
+constexpr int F64_STAGE = TM * KB * 8;  // float64 staging per pipeline stage
 constexpr int kSmemBudget = 220 * 1024;
 
-__host__ __device__ constexpr int stage_bytes(int S) { return S * (TM + TN) * KB * 2; }
-__host__ __device__ constexpr int num_stages(int S) {
-    return kSmemBudget / stage_bytes(S) > 6 ? 6 : kSmemBudget / stage_bytes(S);
+__host__ __device__ constexpr int stage_bytes(int S, bool fused = false) {
+    return S * (TM + TN) * KB * 2 + (fused ? F64_STAGE : 0);
+}
+__host__ __device__ constexpr int num_stages(int S, bool fused = false) {
+    return kSmemBudget / stage_bytes(S, fused) > 6 ? 6 : kSmemBudget / stage_bytes(S, fused);
 }
 // Longest contraction chunk whose group sums stay exact in FP32, in k-blocks.
 __host__ __device__ constexpr int chunk_kblocks(int S) { return (int)(((1 << 24) - 1) / (S * 65 * 65) / KB); }
@@ -289,6 +297,9 @@ struct GemmArgs {
     int64_t* partial;    // splits > 1: [split][tiles_m*TM][tiles_n*TN]
     int splits;
     unsigned int* err;
+    // Fused A: float64 source, element (m, k) at a_f64[(m % a_div) + (m / a_div) * a_s1 + k * a_sk].
+    const double* a_f64;
+    int64_t a_div, a_s1, a_sk, K;
 };
 
 __device__ __forceinline__ double scale_pow2(int64_t v, int ex) {
@@ -320,34 +331,54 @@ __device__ __forceinline__ bool work_item(const GemmArgs& a, int64_t w, int64_t&
     return c0 < c1;
 }
 
+// Several independent products in one launch: their work lists are
+// concatenated (prefix[p] = first work item of problem p).  Passed by value, so
+// a launch captured in a CUDA graph carries its own copy.
+template <int MAXG>
+struct GroupArgs {
+    int n;
+    int64_t prefix[MAXG + 1];
+    GemmArgs a[MAXG];
+};
+constexpr int kMaxGroup = 48;
+
 // Persistent split-precision GEMM: one CTA per SM walks the work list with
 // stride gridDim.x.  Producer and MMA run ahead across tile boundaries; the
 // epilogue hands the tensor memory back as soon as it has read a chunk, so
 // the next chunk's MMAs overlap the previous tile's conversion and stores.
-template <int S>
-__global__ void __launch_bounds__(NTHREADS, 1) oz_gemm_kernel(GemmArgs a) {
-    constexpr int STAGES = num_stages(S);
+template <int S, bool FUSED, int MAXG>
+__global__ void __launch_bounds__(FUSED ? NTHREADS_FUSED : NTHREADS, 1)
+    oz_gemm_kernel(const __grid_constant__ GroupArgs<MAXG> G) {
+    constexpr int STAGES = num_stages(S, FUSED);
     constexpr uint32_t A_BLK = TM * KB * 2;  // one digit plane, bytes
     constexpr uint32_t B_BLK = TN * KB * 2;
     constexpr uint32_t A_STAGE = S * A_BLK;
-    constexpr uint32_t STAGE = S * (A_BLK + B_BLK);
+    constexpr uint32_t DIGITS = S * (A_BLK + B_BLK);
+    constexpr uint32_t STAGE = stage_bytes(S, FUSED);  // digits, then (fused) float64 staging
     constexpr uint32_t NCOLS = tmem_cols(S);
 
     extern __shared__ __align__(1024) uint8_t smem[];
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE);
     uint64_t* empty = full + STAGES;
-    uint64_t* acc_full = empty + STAGES;
+    uint64_t* f64_full = empty + STAGES;   // fused: float64 tile landed
+    uint64_t* f64_empty = f64_full + STAGES;  // fused: converters finished reading it
+    uint64_t* acc_full = f64_empty + STAGES;
     uint64_t* acc_empty = acc_full + 1;
     uint64_t* drain = acc_empty + 1;
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t nitems = a.tiles_m * a.tiles_n * a.splits;
+    const int64_t nitems = G.prefix[G.n];
+    unsigned int* const err = G.a[0].err;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
-            ptx::mbar_init(&full[s], 1);
+            // Fused: the A digits are written by the converter threads, the B
+            // digits by a bulk copy announced with arrive.expect_tx.
+            ptx::mbar_init(&full[s], FUSED ? CONV_THREADS + 1 : 1);
             ptx::mbar_init(&empty[s], 1);
+            ptx::mbar_init(&f64_full[s], 1);
+            ptx::mbar_init(&f64_empty[s], CONV_THREADS);
         }
         ptx::mbar_init(acc_full, 1);
         ptx::mbar_init(acc_empty, EPI_THREADS);
@@ -368,21 +399,59 @@ __global__ void __launch_bounds__(NTHREADS, 1) oz_gemm_kernel(GemmArgs a) {
             // ---------------- producer: bulk copies of pre-tiled digit planes
             int64_t it = 0;
             bool ok = true;
+            int p = 0;
             for (int64_t w = blockIdx.x; w < nitems && ok; w += gridDim.x) {
+                while (w >= G.prefix[p + 1]) ++p;
+                const GemmArgs& a = G.a[p];
                 int64_t tm, tn, c0, c1;
                 int z;
-                if (!work_item(a, w, tm, tn, c0, c1, z)) continue;
+                if (!work_item(a, w - G.prefix[p], tm, tn, c0, c1, z)) continue;
                 const uint8_t* abase = a.a_slices + tm * a.a_tile_stride;
                 const uint8_t* bbase = a.b_slices + (tn >> 1) * a.b_tile2_stride + (tn & 1) * a.b_half_stride;
+                // Fused: the tile's rows m0..m1 split into runs that stay inside one
+                // slab (at most 3 for TM = 128 rows); found once per work item.
+                int nseg = 0;
+                int32_t seg_dst[3] = {0, 0, 0}, seg_len[3] = {0, 0, 0};
+                int64_t seg_src[3] = {0, 0, 0};
+                const int64_t m0 = tm * TM, m1 = min(a.M, m0 + TM);
+                if constexpr (FUSED) {
+                    int64_t q = m0 / a.a_div, rem = m0 - q * a.a_div;
+                    for (int64_t r = m0; r < m1 && nseg < 3;) {
+                        const int64_t re = min(m1, r + (a.a_div - rem));
+                        seg_dst[nseg] = (int32_t)(r - m0);
+                        seg_len[nseg] = (int32_t)((re - r) * 8);
+                        seg_src[nseg] = rem + q * a.a_s1;
+                        ++nseg;
+                        r = re;
+                        ++q;
+                        rem = 0;
+                    }
+                }
                 const int64_t kb1 = min(a.Kb, c1 * a.chunk_kb);
                 for (int64_t kb = c0 * a.chunk_kb; kb < kb1; ++kb, ++it) {
                     const int st = (int)(it % STAGES);
                     const uint32_t ph = (uint32_t)((it / STAGES) & 1);
-                    if (!ptx::mbar_wait(&empty[st], ph ^ 1u, a.err)) { ok = false; break; }
                     uint8_t* sa = smem + st * STAGE;
                     uint8_t* sb = sa + A_STAGE;
-                    ptx::mbar_arrive_expect_tx(&full[st], STAGE);
-                    ptx::bulk_g2s(sa, abase + kb * a.a_kb_stride, A_STAGE, &full[st]);
+                    if constexpr (FUSED) {
+                        // float64 rows m0..m1 for k-rows k0..k1 into the staging buffer [k][TM].
+                        if (!ptx::mbar_wait(&f64_empty[st], ph ^ 1u, a.err)) { ok = false; break; }
+                        double* stg = reinterpret_cast<double*>(sa + DIGITS);
+                        const int64_t k0 = kb * KB, k1 = min(a.K, k0 + KB);
+                        ptx::mbar_arrive_expect_tx(&f64_full[st], (uint32_t)((k1 - k0) * (m1 - m0) * 8));
+                        const double* src = a.a_f64 + k0 * a.a_sk;
+                        for (int64_t k = k0; k < k1; ++k, src += a.a_sk) {
+                            double* dst = stg + (k - k0) * TM;
+                            for (int g = 0; g < nseg; ++g)
+                                ptx::bulk_g2s(dst + seg_dst[g], src + seg_src[g], (uint32_t)seg_len[g], &f64_full[st]);
+                        }
+                        if (!ptx::mbar_wait(&empty[st], ph ^ 1u, a.err)) { ok = false; break; }
+                        ptx::mbar_arrive_expect_tx(&full[st], S * B_BLK);
+                    } else {
+                        if (!ptx::mbar_wait(&empty[st], ph ^ 1u, a.err)) { ok = false; break; }
+                        ptx::mbar_arrive_expect_tx(&full[st], DIGITS);
+                        ptx::bulk_g2s(sa, abase + kb * a.a_kb_stride, A_STAGE, &full[st]);
+                    }
 #pragma unroll
                     for (int s = 0; s < S; ++s)
                         ptx::bulk_g2s(sb + s * B_BLK, bbase + kb * a.b_kb_stride + s * a.b_s_stride, B_BLK, &full[st]);
@@ -390,8 +459,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) oz_gemm_kernel(GemmArgs a) {
             }
             if (!ok) {
                 // Let copies already issued land before the CTA can exit.
-                for (int64_t j = max((int64_t)0, it - STAGES); j < it; ++j)
-                    ptx::mbar_wait(&full[j % STAGES], (uint32_t)((j / STAGES) & 1), a.err);
+                for (int64_t j = max((int64_t)0, it - STAGES); j < it; ++j) {
+                    if (FUSED) ptx::mbar_wait(&f64_full[j % STAGES], (uint32_t)((j / STAGES) & 1), err);
+                    else ptx::mbar_wait(&full[j % STAGES], (uint32_t)((j / STAGES) & 1), err);
+                }
             }
         }
     } else if (warp == 1) {
@@ -402,10 +473,13 @@ __global__ void __launch_bounds__(NTHREADS, 1) oz_gemm_kernel(GemmArgs a) {
             const uint32_t sbase = ptx::smem_u32(smem);
             const uint64_t adesc0 = ptx::smem_desc_kmajor_noswizzle(sbase, kLBO, kSBO);
             const uint64_t bdesc0 = ptx::smem_desc_kmajor_noswizzle(sbase + A_STAGE, kLBO, kSBO);
+            int p = 0;
             for (int64_t w = blockIdx.x; w < nitems && ok; w += gridDim.x) {
+                while (w >= G.prefix[p + 1]) ++p;
+                const GemmArgs& a = G.a[p];
                 int64_t tm, tn, c0, c1;
                 int z;
-                if (!work_item(a, w, tm, tn, c0, c1, z)) continue;
+                if (!work_item(a, w - G.prefix[p], tm, tn, c0, c1, z)) continue;
                 for (int64_t c = c0; c < c1 && ok; ++c, ++cc) {
                     if (cc > 0) {
                         if (!ptx::mbar_wait(acc_empty, (uint32_t)((cc - 1) & 1), a.err)) { ok = false; break; }
@@ -444,7 +518,52 @@ __global__ void __launch_bounds__(NTHREADS, 1) oz_gemm_kernel(GemmArgs a) {
             }
             // Every MMA issued so far has completed once `drain` fires.
             ptx::mma_commit(drain);
-            ptx::mbar_wait(drain, 0, a.err);
+            ptx::mbar_wait(drain, 0, err);
+        }
+    } else if (FUSED && warp >= 10) {
+        // ---------------- converters (fused): float64 staging -> A digit planes
+        const int r = threadIdx.x - EPI_THREADS - 64;  // tile row 0..127
+        int64_t it = 0;
+        bool ok = true;
+        int p = 0;
+        for (int64_t w = blockIdx.x; w < nitems && ok; w += gridDim.x) {
+            while (w >= G.prefix[p + 1]) ++p;
+            const GemmArgs& a = G.a[p];
+            int64_t tm, tn, c0, c1;
+            int z;
+            if (!work_item(a, w - G.prefix[p], tm, tn, c0, c1, z)) continue;
+            const int64_t m = tm * TM + r;
+            const bool valid = m < a.M;
+            const int em = valid ? a.ea[m] : 0;
+            const int64_t kb1 = min(a.Kb, c1 * a.chunk_kb);
+            for (int64_t kb = c0 * a.chunk_kb; kb < kb1; ++kb, ++it) {
+                const int st = (int)(it % STAGES);
+                const uint32_t ph = (uint32_t)((it / STAGES) & 1);
+                uint8_t* sa = smem + st * STAGE;
+                const double* stg = reinterpret_cast<const double*>(sa + DIGITS);
+                if (!ptx::mbar_wait(&f64_full[st], ph, a.err)) { ok = false; break; }
+                const int kv = (int)min((int64_t)KB, a.K - kb * KB);
+                double x0[8], x1[8];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    x0[j] = (valid && j < kv) ? stg[j * TM + r] : 0.0;
+                    x1[j] = (valid && j + 8 < kv) ? stg[(j + 8) * TM + r] : 0.0;
+                }
+                ptx::mbar_arrive(&f64_empty[st]);
+                if (!ptx::mbar_wait(&empty[st], ph ^ 1u, a.err)) { ok = false; break; }
+                uint32_t w0[S][4], w1[S][4];
+                digits8<S>(x0, em, w0);
+                digits8<S>(x1, em, w1);
+#pragma unroll
+                for (int s = 0; s < S; ++s) {
+                    *reinterpret_cast<uint4*>(sa + s * A_BLK + core_offset(r, 0)) =
+                        make_uint4(w0[s][0], w0[s][1], w0[s][2], w0[s][3]);
+                    *reinterpret_cast<uint4*>(sa + s * A_BLK + core_offset(r, 8)) =
+                        make_uint4(w1[s][0], w1[s][1], w1[s][2], w1[s][3]);
+                }
+                ptx::fence_proxy_async_smem();
+                ptx::mbar_arrive(&full[st]);
+            }
         }
     } else {
         // ---------------- epilogue: 8 warps; warp w reads TMEM lane quadrant w % 4
@@ -455,10 +574,13 @@ __global__ void __launch_bounds__(NTHREADS, 1) oz_gemm_kernel(GemmArgs a) {
         const int rl = 32 * q + lane;
         int64_t cc = 0;
         bool ok = true;
+        int p = 0;
         for (int64_t w = blockIdx.x; w < nitems && ok; w += gridDim.x) {
+            while (w >= G.prefix[p + 1]) ++p;
+            const GemmArgs& a = G.a[p];
             int64_t tm, tn, c0, c1;
             int z;
-            if (!work_item(a, w, tm, tn, c0, c1, z)) continue;
+            if (!work_item(a, w - G.prefix[p], tm, tn, c0, c1, z)) continue;
             const int64_t m = tm * TM + rl;
             int64_t acc[HC];
 #pragma unroll
@@ -562,8 +684,22 @@ __global__ void mirror_kernel(OutMap o, int64_t N) {
 
 template <int S>
 void set_smem_attr() {
-    constexpr int bytes = num_stages(S) * stage_bytes(S) + 256;
-    cudaFuncSetAttribute(oz_gemm_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    const int plain = num_stages(S, false) * stage_bytes(S, false) + 256;
+    const int fused = num_stages(S, true) * stage_bytes(S, true) + 256;
+    cudaFuncSetAttribute(oz_gemm_kernel<S, false, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, plain);
+    cudaFuncSetAttribute(oz_gemm_kernel<S, true, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, fused);
+    cudaFuncSetAttribute(oz_gemm_kernel<S, false, kMaxGroup>, cudaFuncAttributeMaxDynamicSharedMemorySize, plain);
+    cudaFuncSetAttribute(oz_gemm_kernel<S, true, kMaxGroup>, cudaFuncAttributeMaxDynamicSharedMemorySize, fused);
+}
+
+// The fused path streams A's float64 rows with 1-D bulk copies: every run of
+// rows must start 16-byte aligned and have an even length.
+// A tile's 128 rows must also fall into at most 3 such runs (runs of at least
+// 64 rows), the size of the producer's per-tile run table.
+bool can_fuse_a(const OzOperand& A, bool reuse) {
+    const bool short_runs = A.div < A.rows;
+    return !reuse && A.s0 == 1 && A.sk != 1 && (!short_runs || (A.div % 2 == 0 && A.div >= TM / 2)) &&
+           A.s1 % 2 == 0 && A.sk % 2 == 0 && A.rows % 2 == 0 && ((uintptr_t)A.p % 16) == 0 && A.rows >= TM;
 }
 
 struct Sliced {
@@ -571,6 +707,19 @@ struct Sliced {
     int64_t tiles = 0, Kb = 0;
     int T = 0;
 };
+
+// Per-row biased exponent maxima only (for the fused path, whose digits are
+// formed inside the GEMM).
+template <int S>
+rt_status row_exponents(const Operand& op, int64_t K, int* emax, cudaStream_t stream) {
+    unsigned int* err = error_word_device();
+    RT_REQUIRE(err != nullptr, "oz: device error word unavailable");
+    RT_CUDA_TRY(cudaMemsetAsync(emax, 0, sizeof(int) * (size_t)op.rows, stream));
+    const int64_t kspan = 512;
+    dim3 g1((unsigned)ceil_div(op.rows, 256), (unsigned)ceil_div(K, kspan));
+    emax_strided_kernel<<<g1, 256, 0, stream>>>(op, K, kspan, emax, err);
+    return check_launch("emax_strided_kernel");
+}
 
 template <int S>
 rt_status slice_operand(const Operand& op, int64_t K, int T, Sliced& out, cudaStream_t stream) {
@@ -608,25 +757,65 @@ rt_status slice_operand(const Operand& op, int64_t K, int T, Sliced& out, cudaSt
     return RT_OK;
 }
 
+// One product ready to launch: its digit planes (or, fused, A's row
+// exponents), split-K partials and kernel arguments.
+struct Prepared {
+    Sliced sa, sb;
+    ScratchBuf part;
+    GemmArgs a{};
+    bool fused = false;
+    int64_t items = 0;    // work items (tiles x splits)
+    int64_t active = 0;   // output tiles that carry work (upper triangle when symmetric)
+    int chunks_per_item = 0;
+    double flops = 0.0;   // algorithmic digit-pair tensor work
+};
+
 template <int S>
-rt_status run(const OzGemm& g, cudaStream_t stream) {
-    static bool attr_done = false;
-    if (!attr_done) {
+void ensure_attrs() {
+    static bool done = false;
+    if (!done) {
         set_smem_attr<S>();
-        attr_done = true;
+        done = true;
     }
+}
+
+// Slicing and argument set-up for one product; the GEMM itself is launched by
+// launch_group, possibly together with other products.
+template <int S>
+rt_status prepare(const OzGemm& g, Prepared& P, cudaStream_t stream) {
+    ensure_attrs<S>();
     Operand A{g.A.p, g.A.rows, g.A.div, g.A.s0, g.A.s1, g.A.sk};
     Operand B{g.B.p, g.B.rows, g.B.div, g.B.s0, g.B.s1, g.B.sk};
-    Sliced sa, sb;
+    Sliced& sa = P.sa;
+    Sliced& sb = P.sb;
     const bool reuse = g.b_is_a;
-    // Slicing is HBM-bound: count bytes (8 read + 2*S written per element).
-    const double slice_bytes = (double)(A.rows + (reuse ? 0 : B.rows)) * (double)g.K * (8.0 + 2.0 * S);
+    const bool fused = g.allow_fuse && can_fuse_a(g.A, reuse);
+    P.fused = fused;
+    // Slicing is HBM-bound: count bytes (8 read + 2*S written per element; the
+    // fused path only reads A's float64 once for its row exponents).
+    const double slice_bytes = fused ? (double)A.rows * g.K * 8.0 + (double)B.rows * g.K * (8.0 + 2.0 * S)
+                                     : (double)(A.rows + (reuse ? 0 : B.rows)) * (double)g.K * (8.0 + 2.0 * S);
     prof_begin(PROF_OZ_SLICE, stream);
-    RT_TRY(slice_operand<S>(A, g.K, TM, sa, stream));
+    if (fused) {
+        sa.T = TM;
+        sa.tiles = ceil_div(A.rows, TM);
+        sa.Kb = ceil_div(g.K, KB);
+        RT_TRY(scratch_alloc(sa.emax, sizeof(int) * (size_t)A.rows, stream));
+        RT_TRY(row_exponents<S>(A, g.K, sa.emax.as<int>(), stream));
+    } else {
+        RT_TRY(slice_operand<S>(A, g.K, TM, sa, stream));
+    }
     if (!reuse) RT_TRY(slice_operand<S>(B, g.K, TN, sb, stream));
     prof_end(PROF_OZ_SLICE, stream, slice_bytes);
 
-    GemmArgs a{};
+    GemmArgs& a = P.a;
+    if (fused) {
+        a.a_f64 = A.p;
+        a.a_div = A.div;
+        a.a_s1 = A.s1;
+        a.a_sk = A.sk;
+    }
+    a.K = g.K;
     a.a_slices = sa.planes.as<uint8_t>();
     a.a_s_stride = TM * KB * 2;
     a.a_kb_stride = (int64_t)S * TM * KB * 2;
@@ -658,26 +847,38 @@ rt_status run(const OzGemm& g, cudaStream_t stream) {
     a.out = OutMap{g.C.p, g.C.md, g.C.ms0, g.C.ms1, g.C.nd, g.C.ns0, g.C.ns1};
     a.err = error_word_device();
 
-    // Split the chunk range across CTAs when there are too few tiles to fill the
-    // GPU; pick the split count whose CTA total best fills whole waves.
-    const int64_t tiles = a.tiles_m * a.tiles_n;
-    int64_t active = tiles;
+    int64_t active = a.tiles_m * a.tiles_n;
     if (g.symmetric) {
         active = 0;
         for (int64_t tm = 0; tm < a.tiles_m; ++tm)
             for (int64_t tn = 0; tn < a.tiles_n; ++tn)
                 if (tn * TN + TN - 1 >= tm * TM) ++active;
     }
+    P.active = active;
+    P.chunks_per_item = g.chunks_per_item;
+    P.flops = 2.0 * (double)a.M * (double)a.N * (double)g.K * (g.symmetric ? 0.5 : 1.0) * S * (S + 1) / 2;
+    return RT_OK;
+}
+
+// Split-K plan of one prepared product.  group_active is the number of active
+// output tiles of every product that shares the launch: the chunk range is
+// split across CTAs only when the whole launch has too few tiles to fill the
+// GPU, with the split count whose CTA total best fills whole waves.
+template <int S>
+rt_status plan(Prepared& P, int64_t group_active, cudaStream_t stream) {
+    GemmArgs& a = P.a;
+    const int64_t tiles = a.tiles_m * a.tiles_n;
     int64_t splits = 1;
     const int64_t sms = sm_count();
-    if (active < sms && a.nchunks > 1) {
+    if (group_active < sms && a.nchunks > 1) {
         double best = 0.0;
         for (int64_t w = 1; w <= 4; ++w) {
-            const int64_t sp = std::min<int64_t>(a.nchunks, std::max<int64_t>(1, (w * sms) / active));
-            const double eff = (double)(active * sp) / (double)(ceil_div(active * sp, sms) * sms);
+            const int64_t sp = std::min<int64_t>(a.nchunks, std::max<int64_t>(1, (w * sms) / group_active));
+            const double eff = (double)(group_active * sp) / (double)(ceil_div(group_active * sp, sms) * sms);
             if (eff > best + 0.02) { best = eff; splits = sp; }
         }
     }
+    if (P.chunks_per_item > 0) splits = ceil_div(a.nchunks, (int64_t)P.chunks_per_item);
     a.chunks_per_split = (int)ceil_div(a.nchunks, splits);
     splits = ceil_div(a.nchunks, a.chunks_per_split);
     a.splits = (int)splits;
@@ -690,33 +891,113 @@ rt_status run(const OzGemm& g, cudaStream_t stream) {
         const int need = (int)std::ceil(std::log2(terms * 4292.0)) + 7 * (S - 1) - 62;
         a.R = std::max(0, need);
     }
-
-    ScratchBuf part;
     if (splits > 1) {
-        RT_TRY(scratch_alloc(part, sizeof(int64_t) * (size_t)splits * a.tiles_m * TM * a.tiles_n * TN, stream));
-        a.partial = part.as<int64_t>();
+        RT_TRY(scratch_alloc(P.part, sizeof(int64_t) * (size_t)splits * a.tiles_m * TM * a.tiles_n * TN, stream));
+        a.partial = P.part.as<int64_t>();
     }
-    constexpr int smem = num_stages(S) * stage_bytes(S) + 256;
-    dim3 grid((unsigned)std::min<int64_t>(tiles * splits, sms));
-    // Algorithmic tensor work: S(S+1)/2 digit-pair products of 2*M*N*K each
-    // (half of the square for the symmetric product).
-    const double pair_flops = 2.0 * (double)a.M * (double)a.N * (double)g.K * (g.symmetric ? 0.5 : 1.0);
+    P.items = tiles * splits;
+    return RT_OK;
+}
+
+// One persistent launch over the work items of n prepared products (all of
+// the same fused mode).
+template <int S, int MAXG>
+rt_status launch_group(Prepared* const* ps, int n, cudaStream_t stream) {
+    static_assert(sizeof(GroupArgs<MAXG>) <= 32000, "kernel parameter block too large");
+    GroupArgs<MAXG> G;
+    G.n = n;
+    G.prefix[0] = 0;
+    double flops = 0.0;
+    for (int i = 0; i < n; ++i) {
+        G.a[i] = ps[i]->a;
+        G.prefix[i + 1] = G.prefix[i] + ps[i]->items;
+        flops += ps[i]->flops;
+    }
+    for (int i = n; i < MAXG; ++i) G.prefix[i + 1] = G.prefix[n];
+    if (G.prefix[n] == 0) return RT_OK;
+    const bool fused = ps[0]->fused;
+    dim3 grid((unsigned)std::min<int64_t>(G.prefix[n], sm_count()));
     prof_begin(PROF_OZ_GEMM, stream);
-    oz_gemm_kernel<S><<<grid, NTHREADS, smem, stream>>>(a);
-    prof_end(PROF_OZ_GEMM, stream, pair_flops * S * (S + 1) / 2);
-    RT_TRY(check_launch("oz_gemm_kernel"));
-    if (splits > 1) {
-        oz_finalize_kernel<S><<<4 * sm_count(), 256, 0, stream>>>(a);
+    if (fused)
+        oz_gemm_kernel<S, true, MAXG>
+            <<<grid, NTHREADS_FUSED, num_stages(S, true) * stage_bytes(S, true) + 256, stream>>>(G);
+    else
+        oz_gemm_kernel<S, false, MAXG>
+            <<<grid, NTHREADS, num_stages(S, false) * stage_bytes(S, false) + 256, stream>>>(G);
+    prof_end(PROF_OZ_GEMM, stream, flops);
+    return check_launch("oz_gemm_kernel");
+}
+
+// Split-K reduction and symmetric mirror of one product.
+template <int S>
+rt_status finish(const Prepared& P, cudaStream_t stream) {
+    if (P.a.splits > 1) {
+        oz_finalize_kernel<S><<<4 * sm_count(), 256, 0, stream>>>(P.a);
         RT_TRY(check_launch("oz_finalize_kernel"));
     }
-    if (g.symmetric) {
-        mirror_kernel<<<4 * sm_count(), 256, 0, stream>>>(a.out, a.M);
+    if (P.a.symmetric) {
+        mirror_kernel<<<4 * sm_count(), 256, 0, stream>>>(P.a.out, P.a.M);
         RT_TRY(check_launch("mirror_kernel"));
     }
     return RT_OK;
 }
 
+template <int S>
+rt_status run(const OzGemm& g, cudaStream_t stream) {
+    Prepared P;
+    RT_TRY(prepare<S>(g, P, stream));
+    RT_TRY(plan<S>(P, P.active, stream));
+    Prepared* ps[1] = {&P};
+    RT_TRY((launch_group<S, 1>(ps, 1, stream)));
+    return finish<S>(P, stream);
+}
+
+// Many products, grouped into as few launches as possible.
+template <int S>
+rt_status run_many(const OzGemm* gs, int n, cudaStream_t stream) {
+    std::vector<Prepared> P(n);
+    int64_t active = 0;
+    for (int i = 0; i < n; ++i) {
+        RT_TRY(prepare<S>(gs[i], P[i], stream));
+        active += P[i].active;
+    }
+    for (int i = 0; i < n; ++i) RT_TRY(plan<S>(P[i], active, stream));
+    for (int mode = 0; mode < 2; ++mode) {
+        std::vector<Prepared*> grp;
+        for (int i = 0; i < n; ++i)
+            if ((int)P[i].fused == mode && P[i].items > 0) grp.push_back(&P[i]);
+        for (size_t i0 = 0; i0 < grp.size(); i0 += kMaxGroup) {
+            const int cnt = (int)std::min<size_t>(kMaxGroup, grp.size() - i0);
+            RT_TRY((launch_group<S, kMaxGroup>(grp.data() + i0, cnt, stream)));
+        }
+    }
+    for (int i = 0; i < n; ++i) RT_TRY(finish<S>(P[i], stream));
+    return RT_OK;
+}
+
 }  // namespace oz
+
+rt_status oz_gemm_many(const OzGemm* gs, int n, cudaStream_t stream) {
+    if (n <= 0) return RT_OK;
+    const int S = gs[0].nslices;
+    for (int i = 0; i < n; ++i) {
+        RT_REQUIRE(gs[i].nslices == S, "oz_gemm_many: all products need the same slice count");
+        RT_REQUIRE(gs[i].A.rows > 0 && gs[i].B.rows > 0 && gs[i].K > 0, "oz_gemm_many: empty product");
+        RT_REQUIRE(!gs[i].symmetric || (gs[i].b_is_a && gs[i].A.rows == gs[i].B.rows),
+                   "oz_gemm_many: symmetric needs B == A");
+    }
+    switch (S) {
+        case 3: return oz::run_many<3>(gs, n, stream);
+        case 4: return oz::run_many<4>(gs, n, stream);
+        case 5: return oz::run_many<5>(gs, n, stream);
+        case 6: return oz::run_many<6>(gs, n, stream);
+        case 7: return oz::run_many<7>(gs, n, stream);
+        case 8: return oz::run_many<8>(gs, n, stream);
+        default:
+            set_error(RT_ERR_INVALID_ARG, "nslices must be in 3..8 (got %d)", S);
+            return RT_ERR_INVALID_ARG;
+    }
+}
 
 rt_status oz_gemm(const OzGemm& g, cudaStream_t stream) {
     RT_REQUIRE(g.A.rows >= 0 && g.B.rows >= 0 && g.K >= 0, "oz_gemm: negative size");

@@ -104,6 +104,9 @@ struct GemmF64 {
     int splitk = 1;  // >1: partial sums in scratch, reduced deterministically
 };
 rt_status gemm_f64(const GemmF64& g, cudaStream_t stream);
+// Several float64 GEMMs in one launch per op pair (no split-K; k == 0 is not
+// accepted here).
+rt_status gemm_f64_many(const GemmF64* gs, int n, cudaStream_t stream);
 
 // Split-precision (BF16 digit planes on tcgen05, exact integer
 // recombination) GEMM, written as C(m, n) = sum_k A(m, k) * B(n, k):
@@ -128,7 +131,15 @@ struct OzGemm {
     int nslices = 6;
     bool b_is_a = false;
     bool symmetric = false;
+    // Form A's digits inside the GEMM (no digit-plane scratch for A) when A's
+    // layout allows it.  Off by default: separate slicing is faster on GB300;
+    // the fused form trades speed for memory.
+    bool allow_fuse = false;
+    int chunks_per_item = 0;  // >0: exact chunks per work item (split-K granularity); 0: fill whole waves
 };
 rt_status oz_gemm(const OzGemm& g, cudaStream_t stream);
+// Several independent products with the same slice count: one slicing pass
+// each, then as few grouped persistent GEMM launches as possible.
+rt_status oz_gemm_many(const OzGemm* gs, int n, cudaStream_t stream);
 
 }  // namespace rt

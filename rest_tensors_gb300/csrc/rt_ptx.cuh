@@ -76,6 +76,12 @@ __device__ __forceinline__ void bulk_g2s(void* smem_dst, const void* gmem_src, u
         : "memory");
 }
 
+// Make this thread's generic-proxy shared-memory writes visible to the async
+// proxy (tensor-core operand reads) before signalling them on an mbarrier.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
 // ---------------------------------------------------------------- tcgen05 --
 
 __device__ __forceinline__ void tmem_alloc(uint32_t* smem_result, uint32_t ncols) {
