@@ -222,6 +222,10 @@ rt_status rt_davidson_ri_response(const double* Bov, const double* delta, long l
  * include/rt_synth.h (slabs P0..P0+nslab-1 of the full tensor, stored from B). */
 rt_status rt_synth_ri3ao(uint64_t seed, int nb, int P0, int nslab, double* B, void* stream);
 
+/* Fill d[nov] with the synthetic orbital-energy-difference diagonal of the
+ * response problem (rt_delta_elem of include/rt_synth.h, uniform in [0.5, 3.0]). */
+rt_status rt_synth_delta(uint64_t seed, long long nov, double* d, void* stream);
+
 /* Fill M[nb, nb] with the N(0,1) matrix whose QR factor gives the synthetic
  * orbital coefficients (include/rt_synth.h, rt_coef_seed_elem). */
 rt_status rt_synth_coef_seed(uint64_t seed, int nb, double* M, void* stream);

@@ -70,7 +70,8 @@ RT_SYNTH_FN double rt_coef_seed_elem(uint64_t seed, int64_t row, int64_t col) {
 /* Orbital-energy-difference diagonal for the response problem, U[0.5, 3.0]. */
 RT_SYNTH_FN double rt_delta_elem(uint64_t seed, int64_t ia) {
     uint64_t k = rt_splitmix64(seed ^ rt_splitmix64(0x44656C74ull ^ rt_splitmix64((uint64_t)ia)));
-    return 0.5 + 2.5 * (rt_u01(k) - 0x1p-53);
+    /* fused multiply-add: one rounding, the same on the host and the device */
+    return fma(2.5, rt_u01(k) - 0x1p-53, 0.5);
 }
 
 #endif /* RT_SYNTH_H */

@@ -103,6 +103,8 @@ def lib() -> ctypes.CDLL:
     L.rt_ri_exchange_energy.argtypes = [vp, vp, c_int, vp, vp]
     L.rt_synth_ri3ao.restype = c_int
     L.rt_synth_ri3ao.argtypes = [ctypes.c_uint64, c_int, c_int, c_int, vp, vp]
+    L.rt_synth_delta.restype = c_int
+    L.rt_synth_delta.argtypes = [ctypes.c_uint64, ctypes.c_longlong, vp, vp]
     L.rt_synth_coef_seed.restype = c_int
     L.rt_synth_coef_seed.argtypes = [ctypes.c_uint64, c_int, vp, vp]
     L.rt_launch_count.restype = ctypes.c_longlong
@@ -391,6 +393,15 @@ def synth_ri3ao(seed: int, nb: int, naux: int, P0: int = 0, out=None, stream=Non
         out = torch.empty(nb * nb * naux, dtype=torch.float64, device="cuda")
     _check(lib().rt_synth_ri3ao(seed, nb, P0, naux, _dptr(out), _stream(stream)))
     return out
+
+
+def synth_delta(seed: int, nov: int, stream=None):
+    """Device copy of the synthetic orbital-energy-difference diagonal (uniform in [0.5, 3.0])."""
+    import torch
+
+    d = torch.empty(max(nov, 1), dtype=torch.float64, device="cuda")
+    _check(lib().rt_synth_delta(seed, nov, _dptr(d), _stream(stream)))
+    return d[:nov]
 
 
 def synth_coef(seed: int, nb: int, stream=None):

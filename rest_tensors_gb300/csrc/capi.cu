@@ -14,6 +14,7 @@ rt_status ri_j_fp64(const double* B, const double* D, int nb, int naux, double* 
 rt_status exchange_energy(const double* D, const double* K, int nb, double* out, cudaStream_t stream);
 rt_status synth_ri3ao(uint64_t seed, int nb, int P0, int nslab, double* B, cudaStream_t stream);
 rt_status synth_coef_seed(uint64_t seed, int nb, double* M, cudaStream_t stream);
+rt_status synth_delta(uint64_t seed, int64_t nov, double* d, cudaStream_t stream);
 rt_status ri_ao2mo_fp64(const double* C, const double* B, double* R, int nb, int ns, int naux, cudaStream_t stream);
 rt_status ri_ov_k_fp64(const double* C, const double* B, int nb, int naux, int nocc, int nvir, double* ov,
                        double* K, cudaStream_t stream);
@@ -353,6 +354,11 @@ rt_status rt_ri_exchange_energy(const double* D, const double* K, int nb, double
 rt_status rt_synth_ri3ao(uint64_t seed, int nb, int P0, int nslab, double* B, void* stream) {
     RT_REQUIRE(nb >= 0 && P0 >= 0 && nslab >= 0, "rt_synth_ri3ao: negative argument");
     return synth_ri3ao(seed, nb, P0, nslab, B, (cudaStream_t)stream);
+}
+
+rt_status rt_synth_delta(uint64_t seed, long long nov, double* d, void* stream) {
+    RT_REQUIRE(nov >= 0 && (nov == 0 || d), "rt_synth_delta: bad arguments");
+    return synth_delta(seed, nov, d, (cudaStream_t)stream);
 }
 
 rt_status rt_synth_coef_seed(uint64_t seed, int nb, double* M, void* stream) {

@@ -424,6 +424,17 @@ rt_status synth_ri3ao(uint64_t seed, int nb, int P0, int nslab, double* B, cudaS
     return check_launch("synth_kernel");
 }
 
+__global__ void synth_delta_kernel(uint64_t seed, int64_t nov, double* d) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nov; i += (int64_t)gridDim.x * blockDim.x)
+        d[i] = rt_delta_elem(seed, i);
+}
+
+rt_status synth_delta(uint64_t seed, int64_t nov, double* d, cudaStream_t stream) {
+    if (nov == 0) return RT_OK;
+    synth_delta_kernel<<<2 * sm_count(), 256, 0, stream>>>(seed, nov, d);
+    return check_launch("synth_delta_kernel");
+}
+
 rt_status synth_coef_seed(uint64_t seed, int nb, double* M, cudaStream_t stream) {
     if (nb <= 0) return RT_OK;
     synth_coef_kernel<<<sm_count(), 256, 0, stream>>>(seed, nb, M);

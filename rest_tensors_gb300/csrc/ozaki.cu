@@ -316,16 +316,38 @@ __device__ __forceinline__ int64_t out_addr(const OutMap& o, int64_t m, int64_t 
     return (m % o.md) * o.ms0 + (m / o.md) * o.ms1 + (n % o.nd) * o.ns0 + (n / o.nd) * o.ns1;
 }
 
+// First column tile of row tile tm that reaches the diagonal (symmetric products
+// compute only tiles with tn * TN + TN - 1 >= tm * TM).
+__host__ __device__ __forceinline__ int64_t sym_first_tn(int64_t tm) {
+    const int64_t lo = tm * TM - TN + 1;
+    return lo > 0 ? (lo + TN - 1) / TN : 0;
+}
+
 // Work item w of the persistent grid: tile (tm, tn) and split z; false if the
-// item has nothing to do (below the diagonal of a symmetric product, or an
-// empty chunk range).
+// item has nothing to do (an empty chunk range).  A symmetric product lists only
+// its tiles on or above the diagonal, row by row, so every item carries work and
+// consecutive CTAs get equal shares.
 __device__ __forceinline__ bool work_item(const GemmArgs& a, int64_t w, int64_t& tm, int64_t& tn, int64_t& c0,
                                           int64_t& c1, int& z) {
-    const int64_t tile = w / a.splits;
+    int64_t tile = w / a.splits;
     z = (int)(w % a.splits);
-    tn = tile % a.tiles_n;
-    tm = tile / a.tiles_n;
-    if (a.symmetric && (tn * TN + TN - 1) < tm * TM) return false;
+    if (a.symmetric) {
+        tm = 0;
+        for (;;) {
+            const int64_t first = sym_first_tn(tm);
+            const int64_t cnt = a.tiles_n > first ? a.tiles_n - first : 0;
+            if (tile < cnt || tm + 1 >= a.tiles_m) {
+                tn = first + tile;
+                break;
+            }
+            tile -= cnt;
+            ++tm;
+        }
+        if (tn >= a.tiles_n) return false;
+    } else {
+        tn = tile % a.tiles_n;
+        tm = tile / a.tiles_n;
+    }
     c0 = (int64_t)z * a.chunks_per_split;
     c1 = min(a.nchunks, c0 + a.chunks_per_split);
     return c0 < c1;
@@ -452,9 +474,16 @@ __global__ void __launch_bounds__(FUSED ? NTHREADS_FUSED : NTHREADS, 1)
                         ptx::mbar_arrive_expect_tx(&full[st], DIGITS);
                         ptx::bulk_g2s(sa, abase + kb * a.a_kb_stride, A_STAGE, &full[st]);
                     }
+                    // B's digit planes of one k-block are contiguous unless B is A's own
+                    // 128-row tiles (a product with itself): one copy, else one per plane.
+                    if (a.b_s_stride == B_BLK) {
+                        ptx::bulk_g2s(sb, bbase + kb * a.b_kb_stride, S * B_BLK, &full[st]);
+                    } else {
 #pragma unroll
-                    for (int s = 0; s < S; ++s)
-                        ptx::bulk_g2s(sb + s * B_BLK, bbase + kb * a.b_kb_stride + s * a.b_s_stride, B_BLK, &full[st]);
+                        for (int s = 0; s < S; ++s)
+                            ptx::bulk_g2s(sb + s * B_BLK, bbase + kb * a.b_kb_stride + s * a.b_s_stride, B_BLK,
+                                          &full[st]);
+                    }
                 }
             }
             if (!ok) {
@@ -850,9 +879,7 @@ rt_status prepare(const OzGemm& g, Prepared& P, cudaStream_t stream) {
     int64_t active = a.tiles_m * a.tiles_n;
     if (g.symmetric) {
         active = 0;
-        for (int64_t tm = 0; tm < a.tiles_m; ++tm)
-            for (int64_t tn = 0; tn < a.tiles_n; ++tn)
-                if (tn * TN + TN - 1 >= tm * TM) ++active;
+        for (int64_t tm = 0; tm < a.tiles_m; ++tm) active += std::max<int64_t>(0, a.tiles_n - sym_first_tn(tm));
     }
     P.active = active;
     P.chunks_per_item = g.chunks_per_item;
@@ -867,7 +894,7 @@ rt_status prepare(const OzGemm& g, Prepared& P, cudaStream_t stream) {
 template <int S>
 rt_status plan(Prepared& P, int64_t group_active, cudaStream_t stream) {
     GemmArgs& a = P.a;
-    const int64_t tiles = a.tiles_m * a.tiles_n;
+    const int64_t tiles = P.active;
     int64_t splits = 1;
     const int64_t sms = sm_count();
     if (group_active < sms && a.nchunks > 1) {
