@@ -240,6 +240,55 @@ __global__ void __launch_bounds__(256) slice_strided_kernel(SliceArgs a) {
     }
 }
 
+// Strided rows (s0 == 1) with a short contraction (K <= 128 * NBLK): row
+// exponents and digits in one pass.  A CTA covers 16 rows and all of k; each
+// thread keeps its NBLK runs of 8 consecutive k in registers, the 16 threads of
+// a row reduce its exponent maximum, then every thread slices its runs.
+// Replaces emax_strided_kernel + slice_strided_kernel (one read of the operand
+// instead of two); rows beyond the operand (tile padding) get zero digits.
+constexpr int kFusedRows = 16;
+template <int S, int NBLK>
+__global__ void __launch_bounds__(256, 2) slice_strided_rowmax_kernel(SliceArgs a, int* __restrict__ emax_out) {
+    __shared__ unsigned int red[8][kFusedRows];
+    const int r = threadIdx.x & (kFusedRows - 1);
+    const int kq = threadIdx.x >> 4;  // 0..15
+    const int64_t row = (int64_t)blockIdx.x * kFusedRows + r;
+    const bool valid = row < a.src.rows;
+    const double* base = valid ? a.src.p + (row % a.src.div) * a.src.s0 + (row / a.src.div) * a.src.s1 : nullptr;
+    double x[NBLK][8];
+    unsigned int m = 0;
+#pragma unroll
+    for (int j = 0; j < NBLK; ++j) {
+        const int64_t k0 = (int64_t)(kq + 16 * j) * 8;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const int64_t k = k0 + i;
+            x[j][i] = (valid && k < a.K) ? base[k * a.src.sk] : 0.0;
+            m = max(m, ((unsigned int)__double2hiint(x[j][i]) >> 20) & 0x7FFu);
+        }
+    }
+    // threads r and r + 16 of a warp share the row; then across the 8 warps
+    m = max(m, __shfl_xor_sync(0xffffffffu, m, 16));
+    if ((threadIdx.x & 31) < kFusedRows) red[threadIdx.x >> 5][r] = m;
+    __syncthreads();
+#pragma unroll
+    for (int w = 0; w < 8; ++w) m = max(m, red[w][r]);
+    if (valid && kq == 0) {
+        if (m == 0x7FFu) atomicOr(a.err, DEV_ERR_NONFINITE);
+        emax_out[row] = (int)m;
+    }
+    const int64_t tile = row / a.T;
+    const int rt_ = (int)(row % a.T);
+#pragma unroll
+    for (int j = 0; j < NBLK; ++j) {
+        const int64_t k0 = (int64_t)(kq + 16 * j) * 8;
+        if (k0 >= a.Kb * KB) continue;
+        uint32_t w[S][4];
+        digits8<S>(x[j], (int)m, w);
+        store8<S>(a, tile, k0 / KB, rt_, (int)(k0 & (KB - 1)), w);
+    }
+}
+
 // Contiguous rows (sk == 1): the [T x 32] tile is staged through shared
 // memory with coalesced row reads, then sliced as above.
 template <int S>
@@ -770,6 +819,16 @@ rt_status slice_operand(const Operand& op, int64_t K, int T, Sliced& out, cudaSt
         dim3 grid((unsigned)out.tiles, (unsigned)ceil_div(K, SK));
         slice_contig_kernel<S><<<grid, 256, 0, stream>>>(sa);
         RT_TRY(check_launch("slice_contig_kernel"));
+    } else if (op.s0 == 1 && out.Kb * KB <= 128 * 5) {
+        const unsigned grid = (unsigned)(out.tiles * T / kFusedRows);
+        switch ((int)ceil_div(out.Kb, 8)) {
+            case 1: slice_strided_rowmax_kernel<S, 1><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
+            case 2: slice_strided_rowmax_kernel<S, 2><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
+            case 3: slice_strided_rowmax_kernel<S, 3><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
+            case 4: slice_strided_rowmax_kernel<S, 4><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
+            default: slice_strided_rowmax_kernel<S, 5><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
+        }
+        RT_TRY(check_launch("slice_strided_rowmax_kernel"));
     } else if (op.s0 == 1) {
         RT_CUDA_TRY(cudaMemsetAsync(out.emax.p, 0, sizeof(int) * (size_t)op.rows, stream));
         const int64_t kspan = 512;
