@@ -47,8 +47,10 @@ constexpr int TM = 128;        // rows of A per tile (UMMA M)
 constexpr int TN = 64;         // rows of B per tile (UMMA N)
 constexpr int KB = 16;         // k elements per pipeline stage (one MMA k-step)
 constexpr int SK = 32;         // k elements one slicing CTA covers (two k-blocks)
-constexpr int NTHREADS = 320;  // warp 0 producer, warp 1 MMA, warps 2..9 epilogue
-constexpr int EPI_THREADS = 256;
+// warp 0 producer, warp 1 MMA, warps 2.. epilogue (16 warps; 8 in the fused form)
+constexpr int epi_warps(bool fused) { return fused ? 8 : 16; }
+constexpr int NTHREADS = 64 + 32 * epi_warps(false);
+constexpr int EPI_THREADS = 256;  // fused form
 // Fused variant: warps 10..13 turn float64 tiles staged in shared memory into
 // the A digit planes.
 constexpr int NTHREADS_FUSED = 448;
@@ -452,7 +454,7 @@ __global__ void __launch_bounds__(FUSED ? NTHREADS_FUSED : NTHREADS, 1)
             ptx::mbar_init(&f64_empty[s], CONV_THREADS);
         }
         ptx::mbar_init(acc_full, 1);
-        ptx::mbar_init(acc_empty, EPI_THREADS);
+        ptx::mbar_init(acc_empty, 32 * epi_warps(FUSED));
         ptx::mbar_init(drain, 1);
         ptx::fence_mbar_init();
     }
@@ -644,9 +646,10 @@ __global__ void __launch_bounds__(FUSED ? NTHREADS_FUSED : NTHREADS, 1)
             }
         }
     } else {
-        // ---------------- epilogue: 8 warps; warp w reads TMEM lane quadrant w % 4
-        // (its hardware-assigned lanes) and one half of the 64 columns.
-        constexpr int HC = TN / 2;
+        // ---------------- epilogue: warp w reads TMEM lane quadrant w % 4 (its
+        // hardware-assigned lanes) and one of epi_warps / 4 column slices.
+        constexpr int HC = TN / (epi_warps(FUSED) / 4);
+        static_assert(HC % 16 == 0, "column slice must be whole 16-column loads");
         const int q = warp & 3;
         const int h = (warp - 2) >> 2;
         const int rl = 32 * q + lane;
@@ -672,7 +675,7 @@ __global__ void __launch_bounds__(FUSED ? NTHREADS_FUSED : NTHREADS, 1)
                     uint32_t r0[16], r1[16];
                     const uint32_t col = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(g * TN + h * HC);
                     ptx::tmem_ld16(col, r0);
-                    ptx::tmem_ld16(col + 16, r1);
+                    if constexpr (HC > 16) ptx::tmem_ld16(col + 16, r1);
                     ptx::tmem_wait_ld();
                     if (sh >= 0) {
 #pragma unroll
