@@ -291,6 +291,56 @@ __global__ void __launch_bounds__(256, 2) slice_strided_rowmax_kernel(SliceArgs 
     }
 }
 
+// Contiguous rows (sk == 1) with a short contraction (K <= 128 * NBLK): row
+// exponents and digits in one pass.  A CTA covers 16 rows.  Warp w handles rows
+// 8 (w & 1) .. + 7 (lane & 7) and k-groups 4 (w >> 1) + (lane >> 3); each thread
+// keeps NBLK runs of 8 consecutive k (64 contiguous bytes) in registers.  The 16
+// threads of a row (4 lanes x 4 warps) reduce its exponent maximum; then every
+// thread slices its runs.  Stores of one instruction cover 8 rows x 16 bytes.
+template <int S, int NBLK>
+__global__ void __launch_bounds__(256, 2) slice_contig_rowmax_kernel(SliceArgs a, int* __restrict__ emax_out) {
+    __shared__ unsigned int red[4][kFusedRows];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int r = 8 * (warp & 1) + (lane & 7);
+    const int kq = 4 * (warp >> 1) + (lane >> 3);  // 0..15
+    const int64_t row = (int64_t)blockIdx.x * kFusedRows + r;
+    const bool valid = row < a.src.rows;
+    const double* base = valid ? a.src.p + (row % a.src.div) * a.src.s0 + (row / a.src.div) * a.src.s1 : nullptr;
+    double x[NBLK][8];
+    unsigned int m = 0;
+#pragma unroll
+    for (int j = 0; j < NBLK; ++j) {
+        const int64_t k0 = (int64_t)(kq + 16 * j) * 8;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const int64_t k = k0 + i;
+            x[j][i] = (valid && k < a.K) ? base[k] : 0.0;
+            m = max(m, ((unsigned int)__double2hiint(x[j][i]) >> 20) & 0x7FFu);
+        }
+    }
+    // lanes r, r+8, r+16, r+24 share the row within a warp; then 4 warps
+    m = max(m, __shfl_xor_sync(0xffffffffu, m, 8));
+    m = max(m, __shfl_xor_sync(0xffffffffu, m, 16));
+    if (lane < 8) red[warp >> 1][r] = m;
+    __syncthreads();
+#pragma unroll
+    for (int w = 0; w < 4; ++w) m = max(m, red[w][r]);
+    if (valid && kq == 0) {
+        if (m == 0x7FFu) atomicOr(a.err, DEV_ERR_NONFINITE);
+        emax_out[row] = (int)m;
+    }
+    const int64_t tile = row / a.T;
+    const int rt_ = (int)(row % a.T);
+#pragma unroll
+    for (int j = 0; j < NBLK; ++j) {
+        const int64_t k0 = (int64_t)(kq + 16 * j) * 8;
+        if (k0 >= a.Kb * KB) continue;
+        uint32_t w[S][4];
+        digits8<S>(x[j], (int)m, w);
+        store8<S>(a, tile, k0 / KB, rt_, (int)(k0 & (KB - 1)), w);
+    }
+}
+
 // Contiguous rows (sk == 1): the [T x 32] tile is staged through shared
 // memory with coalesced row reads, then sliced as above.
 template <int S>
@@ -815,7 +865,17 @@ rt_status slice_operand(const Operand& op, int64_t K, int T, Sliced& out, cudaSt
     SliceArgs sa{};
     sa.src = op; sa.K = K; sa.T = T; sa.tiles = out.tiles; sa.Kb = out.Kb;
     sa.out = out.planes.as<uint16_t>(); sa.emax = out.emax.as<int>(); sa.err = err;
-    if (op.sk == 1) {
+    if (op.sk == 1 && out.Kb * KB <= 128 * 5) {
+        const unsigned grid = (unsigned)(out.tiles * T / kFusedRows);
+        switch ((int)ceil_div(out.Kb, 8)) {
+            case 1: slice_contig_rowmax_kernel<S, 1><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
+            case 2: slice_contig_rowmax_kernel<S, 2><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
+            case 3: slice_contig_rowmax_kernel<S, 3><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
+            case 4: slice_contig_rowmax_kernel<S, 4><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
+            default: slice_contig_rowmax_kernel<S, 5><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
+        }
+        RT_TRY(check_launch("slice_contig_rowmax_kernel"));
+    } else if (op.sk == 1) {
         const int64_t warps = std::min<int64_t>(op.rows, 64ll * sm_count());
         emax_contig_kernel<<<(unsigned)ceil_div(warps * 32, 256), 256, 0, stream>>>(op, K, out.emax.as<int>(), err);
         RT_TRY(check_launch("emax_contig_kernel"));
