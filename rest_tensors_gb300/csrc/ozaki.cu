@@ -142,9 +142,13 @@ __device__ __forceinline__ void split_digits(double x, int emax, int (&d)[S]) {
     }
 }
 
-// Exact BF16 bit pattern of a small integer (|v| <= 256).
+// Exact BF16 bit pattern of a small integer (|v| <= 256).  The float with bits
+// 0x4B400000 + v is 1.5 * 2^23 + v (for |v| < 2^22), so one FP32 subtraction
+// gives v exactly, without the int-to-float conversion pipe; v has at most 8
+// significant bits, so its BF16 pattern is the float's upper half.
 __device__ __forceinline__ uint32_t bf16_of_int(int v) {
-    return (uint32_t)__float_as_uint((float)v) >> 16;
+    const float f = __int_as_float(0x4B400000 + v) - 12582912.0f;
+    return __float_as_uint(f) >> 16;
 }
 
 // -------------------------------------------------------------- row scale --
