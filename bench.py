@@ -370,6 +370,7 @@ def main():
     import torch
 
     import rest_tensors_gb300 as rt
+    from rest_tensors_gb300 import replicas
 
     torch.cuda.set_device(local)
     dist = None
@@ -407,12 +408,8 @@ def main():
             step(form, nsl)
         e1.record(stream)
         barrier()
-        ms = e0.elapsed_time(e1) / steps
+        ms = replicas.max_over_ranks(e0.elapsed_time(e1) / steps, dev)
         launches = rt.launch_count() - n0
-        if dist is not None:
-            t = torch.tensor([ms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
         return ms, launches
 
     # ---- float64 reference result and its timing
@@ -458,7 +455,7 @@ def main():
     rt.profile_enable(False)
     rt.sync_status()
 
-    value = world * FLOPS / ms / 1e9  # TFLOP/s over all ranks
+    value = replicas.job_throughput([FLOPS] * world, ms * 1e-3) / 1e12  # TFLOP/s over all ranks
     pk, pk_kind = peaks()
     achieved = g_flops / g_ms / 1e9 if g_ms > 0 else None
     peak = pk.get("bf16_tflops_sustained", FALLBACK_PEAKS["bf16_tflops_sustained"])
@@ -489,12 +486,9 @@ def main():
         for _ in range(args.e2e_steps):
             rt.ri_ov_k_host(hC.data_ptr(), hB.data_ptr(), NB, NAUX, NOCC, NVIR, hO.data_ptr(), hK.data_ptr(),
                             form="split", nslices=S, stream=stream)
-        e2e_s = (time.perf_counter() - t0) / args.e2e_steps
-        if dist is not None:
-            t = torch.tensor([e2e_s], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t.item())
-        e2e = {"value": world * FLOPS / e2e_s / 1e12, "unit": "TFLOP/s", "ms_per_step": e2e_s * 1e3,
+        e2e_s = replicas.max_over_ranks((time.perf_counter() - t0) / args.e2e_steps, dev)
+        e2e = {"value": replicas.job_throughput([FLOPS] * world, e2e_s) / 1e12, "unit": "TFLOP/s",
+               "ms_per_step": e2e_s * 1e3,
                "h2d_bytes_per_step": 8 * (NB * NB * NAUX + NB * NB), "d2h_bytes_per_step": 8 * (NOCC * NVIR * NAUX + NB * NB),
                "path": "rt_ri_ov_k_host (C ABI, pinned host buffers, copies inside the timed region)"}
         del hB
