@@ -266,16 +266,21 @@ rt_status rt_ri_ov_k_batched(const rt_ri_problem* probs, int nprob, int form, in
             const rt_ri_problem& q = probs[i];
             if (!live(q)) continue;
             const int64_t per = (int64_t)q.nb * q.nocc;
+            // X = B C_occ as one GEMM over rows (mu, P): A row r at B[r % nb + (r / nb) nb^2],
+            // X row r at X[r % nb + (r / nb) nb nocc].
             GemmF64 a;
-            a.opa = 'N'; a.opb = 'N'; a.m = q.nb; a.n = q.nocc; a.k = q.nb;
-            a.A = q.B; a.lda = q.nb; a.sA = (int64_t)q.nb * q.nb; a.B = q.C; a.ldb = q.nb; a.sB = 0;
-            a.C = X + xoff[i]; a.rsC = 1; a.csC = q.nb; a.bsC = per; a.batch = q.naux;
+            a.opa = 'N'; a.opb = 'N'; a.m = (int64_t)q.nb * q.naux; a.n = q.nocc; a.k = q.nb;
+            a.A = q.B; a.lda = q.nb; a.a_div = q.nb; a.a_s1 = (int64_t)q.nb * q.nb;
+            a.B = q.C; a.ldb = q.nb;
+            a.C = X + xoff[i]; a.rsC = 1; a.csC = q.nb; a.c_md = q.nb; a.c_ms1 = per;
             g1.push_back(a);
             if (q.ov && q.nvir > 0) {
+                // ov = X^T C_vir over rows (i, P): A row r is X[nb r ..]; ov row r at
+                // ov[r % nocc + (r / nocc) nocc nvir].
                 GemmF64 b;
-                b.opa = 'T'; b.opb = 'N'; b.m = q.nocc; b.n = q.nvir; b.k = q.nb;
-                b.A = X + xoff[i]; b.lda = q.nb; b.sA = per; b.B = q.C + per; b.ldb = q.nb; b.sB = 0;
-                b.C = q.ov; b.rsC = 1; b.csC = q.nocc; b.bsC = (int64_t)q.nocc * q.nvir; b.batch = q.naux;
+                b.opa = 'T'; b.opb = 'N'; b.m = (int64_t)q.nocc * q.naux; b.n = q.nvir; b.k = q.nb;
+                b.A = X + xoff[i]; b.lda = q.nb; b.B = q.C + per; b.ldb = q.nb;
+                b.C = q.ov; b.rsC = 1; b.csC = q.nocc; b.c_md = q.nocc; b.c_ms1 = (int64_t)q.nocc * q.nvir;
                 g2.push_back(b);
             }
             if (q.K) {
@@ -283,6 +288,7 @@ rt_status rt_ri_ov_k_batched(const rt_ri_problem* probs, int nprob, int form, in
                 c.opa = 'N'; c.opb = 'T'; c.m = q.nb; c.n = q.nb; c.k = per / q.nb * q.naux;
                 c.A = X + xoff[i]; c.lda = q.nb; c.B = X + xoff[i]; c.ldb = q.nb;
                 c.C = q.K; c.rsC = 1; c.csC = q.nb;
+                c.splitk = (int)std::max<int64_t>(1, c.k / 4096);  // long contractions: ~4096 terms per item
                 g3.push_back(c);
             }
         }

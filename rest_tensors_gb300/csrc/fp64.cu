@@ -7,6 +7,7 @@
 // which every contraction is composed, plus two DFMA streaming kernels for
 // RI-J and a fixed-order reduction for the exchange energy.
 #include <algorithm>
+#include <deque>
 #include <mutex>
 
 #include "rt_internal.cuh"
@@ -32,24 +33,49 @@ struct GemmArgs {
     int splitk;
     int64_t kchunk;
     double* partial;  // splitk > 1: [splitk][batch][m*n]
+    int64_t a_div, a_s1;  // composite A rows (kNoDiv: plain)
+    int64_t c_md, c_ms1;  // composite C rows
 };
 
-// One 64x64 output tile per CTA, 16-deep k slices staged through shared
-// memory, 4x4 outputs per thread.  Thread (tx, ty) owns rows tx + 16*i and
-// columns ty + 16*j, so a warp reads 16 distinct A values and 2 distinct B
-// values per k step (broadcasts, no bank conflicts).
-template <bool TA, bool TB>
+// Offset of A's row gm (opa 'N': element (gm, k) at offset + k*lda; 'T': at offset + k).
+template <bool TA>
+__device__ __forceinline__ int64_t a_row_offset(const GemmArgs& g, int64_t gm) {
+    if (g.a_div == kNoDiv) return TA ? gm * g.lda : gm;
+    const int64_t lo = gm % g.a_div, hi = gm / g.a_div;
+    return (TA ? lo * g.lda : lo) + hi * g.a_s1;
+}
+__device__ __forceinline__ int64_t c_row_offset(const GemmArgs& g, int64_t gm) {
+    if (g.c_md == kNoDiv) return gm * g.rsC;
+    return (gm % g.c_md) * g.rsC + (gm / g.c_md) * g.c_ms1;
+}
+
+// One BMT x BNT output tile per CTA (64x64; 128x32, 32x128, 256x16 or 16x256
+// for a narrow side), 16-deep k slices staged through shared memory, 4x4 outputs per thread.
+// Thread (tx, ty) owns rows tx + TXN*i and columns ty + TYN*j, so a warp reads
+// at most 32 distinct A values and a few distinct B values per k step
+// (broadcasts, no bank conflicts beyond the 2-wavefront double access).
+template <bool TA, bool TB, int BMT, int BNT>
 __device__ __forceinline__ void dgemm_tile_body(const GemmArgs& g, int64_t tile, int64_t b_first, int64_t b_step,
                                                 int split) {
-    __shared__ double As[BK][BM + 1];
-    __shared__ double Bs[BK][BN + 1];
+    constexpr int TXN = BMT / 4, TYN = BNT / 4;
+    static_assert(TXN * TYN == NT, "4x4 outputs per thread");
+    __shared__ double As[BK][BMT + 1];
+    __shared__ double Bs[BK][BNT + 1];
     const int tid = threadIdx.x;
-    const int tx = tid & 15, ty = tid >> 4;
+    const int tx = tid % TXN, ty = tid / TXN;
     const int64_t tm = tile % g.tiles_m, tn = tile / g.tiles_m;
-    const int64_t m0 = tm * BM, n0 = tn * BN;
+    const int64_t m0 = tm * BMT, n0 = tn * BNT;
     const int64_t k0 = (int64_t)split * g.kchunk;
     const int64_t k1 = min(g.k, k0 + g.kchunk);
 
+    // Row offsets of the A elements this thread stages (fixed for the tile).
+    constexpr int RA = (BMT * BK) / NT;
+    int64_t aoff[TA ? RA : 1];
+#pragma unroll
+    for (int r = 0; r < (TA ? RA : 1); ++r) {
+        const int mi = TA ? (tid >> 4) + 16 * r : tid % BMT;
+        aoff[r] = a_row_offset<TA>(g, min(m0 + mi, g.m - 1));
+    }
     for (int64_t b = b_first; b < g.batch; b += b_step) {
         const double* A = g.A + b * g.sA;
         const double* B = g.B + b * g.sB;
@@ -60,23 +86,23 @@ __device__ __forceinline__ void dgemm_tile_body(const GemmArgs& g, int64_t tile,
             for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
 
         for (int64_t kk = k0; kk < k1; kk += BK) {
-            // Stage A tile (BM x BK) as As[k][m].
+            // Stage A tile (BMT x BK) as As[k][m]; consecutive threads read consecutive addresses.
 #pragma unroll
-            for (int r = 0; r < (BM * BK) / NT; ++r) {
+            for (int r = 0; r < (BMT * BK) / NT; ++r) {
                 int mi, ki;
-                if (!TA) { mi = tid & 63; ki = (tid >> 6) + 4 * r; }
+                if (!TA) { mi = tid % BMT; ki = tid / BMT + (NT / BMT) * r; }
                 else { ki = tid & 15; mi = (tid >> 4) + 16 * r; }
                 const int64_t gm = m0 + mi, gk = kk + ki;
                 double v = 0.0;
-                if (gm < g.m && gk < k1) v = TA ? A[gk + gm * g.lda] : A[gm + gk * g.lda];
+                if (gm < g.m && gk < k1) v = TA ? A[aoff[TA ? r : 0] + gk] : A[aoff[0] + gk * g.lda];
                 As[ki][mi] = v;
             }
-            // Stage B tile (BK x BN) as Bs[k][n].
+            // Stage B tile (BK x BNT) as Bs[k][n].
 #pragma unroll
-            for (int r = 0; r < (BN * BK) / NT; ++r) {
+            for (int r = 0; r < (BNT * BK) / NT; ++r) {
                 int ni, ki;
                 if (!TB) { ki = tid & 15; ni = (tid >> 4) + 16 * r; }
-                else { ni = tid & 63; ki = (tid >> 6) + 4 * r; }
+                else { ni = tid % BNT; ki = tid / BNT + (NT / BNT) * r; }
                 const int64_t gn = n0 + ni, gk = kk + ki;
                 double v = 0.0;
                 if (gn < g.n && gk < k1) v = TB ? B[gn + gk * g.ldb] : B[gk + gn * g.ldb];
@@ -87,9 +113,9 @@ __device__ __forceinline__ void dgemm_tile_body(const GemmArgs& g, int64_t tile,
             for (int q = 0; q < BK; ++q) {
                 double a[4], bb[4];
 #pragma unroll
-                for (int i = 0; i < 4; ++i) a[i] = As[q][tx + 16 * i];
+                for (int i = 0; i < 4; ++i) a[i] = As[q][tx + TXN * i];
 #pragma unroll
-                for (int j = 0; j < 4; ++j) bb[j] = Bs[q][ty + 16 * j];
+                for (int j = 0; j < 4; ++j) bb[j] = Bs[q][ty + TYN * j];
 #pragma unroll
                 for (int i = 0; i < 4; ++i)
 #pragma unroll
@@ -100,16 +126,16 @@ __device__ __forceinline__ void dgemm_tile_body(const GemmArgs& g, int64_t tile,
 
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-            const int64_t gm = m0 + tx + 16 * i;
+            const int64_t gm = m0 + tx + TXN * i;
             if (gm >= g.m) continue;
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
-                const int64_t gn = n0 + ty + 16 * j;
+                const int64_t gn = n0 + ty + TYN * j;
                 if (gn >= g.n) continue;
                 if (g.splitk > 1) {
                     g.partial[((int64_t)split * g.batch + b) * g.m * g.n + gm + gn * g.m] = acc[i][j];
                 } else {
-                    double* c = g.C + gm * g.rsC + gn * g.csC + b * g.bsC;
+                    double* c = g.C + c_row_offset(g, gm) + gn * g.csC + b * g.bsC;
                     double v = g.alpha * acc[i][j];
                     if (g.beta != 0.0) v = fma(g.beta, *c, v);
                     *c = v;
@@ -119,13 +145,30 @@ __device__ __forceinline__ void dgemm_tile_body(const GemmArgs& g, int64_t tile,
     }
 }
 
-template <bool TA, bool TB>
-__global__ void __launch_bounds__(NT) dgemm_tile_kernel(GemmArgs g) {
-    dgemm_tile_body<TA, TB>(g, blockIdx.x, blockIdx.y, gridDim.y, blockIdx.z);
+// Tile shapes: 0 = 64x64, 1 = 128x32 (n <= 32), 2 = 32x128 (m <= 32),
+// 3 = 256x16 (n <= 16), 4 = 16x256 (m <= 16).
+constexpr int kShapes = 5;
+constexpr int tile_bm(int shape) {
+    return shape == 1 ? 128 : shape == 2 ? 32 : shape == 3 ? 256 : shape == 4 ? 16 : 64;
+}
+constexpr int tile_bn(int shape) {
+    return shape == 1 ? 32 : shape == 2 ? 128 : shape == 3 ? 16 : shape == 4 ? 256 : 64;
+}
+inline int pick_shape(int64_t m, int64_t n) {
+    if (n <= 16 && m > 64) return 3;
+    if (m <= 16 && n > 64) return 4;
+    if (n <= 32 && m > 32) return 1;
+    if (m <= 32 && n > 32) return 2;
+    return 0;
 }
 
-// Several float64 GEMMs (same op pair) in one launch: block x enumerates
-// (problem, tile, batch item) through the prefix sums of tiles * batch.
+template <bool TA, bool TB, int SH>
+__global__ void __launch_bounds__(NT) dgemm_tile_kernel(GemmArgs g) {
+    dgemm_tile_body<TA, TB, tile_bm(SH), tile_bn(SH)>(g, blockIdx.x, blockIdx.y, gridDim.y, blockIdx.z);
+}
+
+// Several float64 GEMMs (same op pair and tile shape) in one launch: block x
+// enumerates (problem, tile, batch item) through the prefix sums of tiles * batch.
 constexpr int kMaxGroupF64 = 64;
 struct GroupF64 {
     int n;
@@ -133,7 +176,9 @@ struct GroupF64 {
     GemmArgs a[kMaxGroupF64];
 };
 
-template <bool TA, bool TB>
+static_assert(sizeof(GroupF64) <= 32000, "kernel parameter block too large");
+
+template <bool TA, bool TB, int SH>
 __global__ void __launch_bounds__(NT) dgemm_group_kernel(const __grid_constant__ GroupF64 G) {
     const int64_t blk = blockIdx.x;
     int p = 0;
@@ -141,7 +186,48 @@ __global__ void __launch_bounds__(NT) dgemm_group_kernel(const __grid_constant__
     const GemmArgs& g = G.a[p];
     const int64_t local = blk - G.prefix[p];
     const int64_t tiles = g.tiles_m * g.tiles_n;
-    dgemm_tile_body<TA, TB>(g, local % tiles, local / tiles, g.batch, 0);
+    const int64_t per_split = tiles * g.batch;
+    const int64_t rem = local % per_split;
+    dgemm_tile_body<TA, TB, tile_bm(SH), tile_bn(SH)>(g, rem % tiles, rem / tiles, g.batch,
+                                                      (int)(local / per_split));
+}
+
+// Deterministic split-K reduction of several grouped products (those with
+// splitk > 1): block x enumerates their output elements through prefix sums.
+__global__ void dgemm_splitk_reduce_group(const __grid_constant__ GroupF64 G) {
+    const int64_t total = G.prefix[G.n];
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        int p = 0;
+        while (idx >= G.prefix[p + 1]) ++p;
+        const GemmArgs& g = G.a[p];
+        const int64_t e0 = idx - G.prefix[p];
+        const int64_t mn = g.m * g.n;
+        const int64_t b = e0 / mn, e = e0 % mn;
+        const int64_t i = e % g.m, j = e / g.m;
+        double s = 0.0;
+        for (int z = 0; z < g.splitk; ++z) s += g.partial[((int64_t)z * g.batch + b) * mn + e];
+        double* c = g.C + c_row_offset(g, i) + j * g.csC + b * g.bsC;
+        double v = g.alpha * s;
+        if (g.beta != 0.0) v = fma(g.beta, *c, v);
+        *c = v;
+    }
+}
+
+template <int SH>
+void launch_tile(bool ta, bool tb, dim3 grid, const GemmArgs& g, cudaStream_t stream) {
+    if (!ta && !tb) dgemm_tile_kernel<false, false, SH><<<grid, NT, 0, stream>>>(g);
+    else if (ta && !tb) dgemm_tile_kernel<true, false, SH><<<grid, NT, 0, stream>>>(g);
+    else if (!ta && tb) dgemm_tile_kernel<false, true, SH><<<grid, NT, 0, stream>>>(g);
+    else dgemm_tile_kernel<true, true, SH><<<grid, NT, 0, stream>>>(g);
+}
+
+template <int SH>
+void launch_group(bool ta, bool tb, unsigned blocks, const GroupF64& G, cudaStream_t stream) {
+    if (!ta && !tb) dgemm_group_kernel<false, false, SH><<<blocks, NT, 0, stream>>>(G);
+    else if (ta && !tb) dgemm_group_kernel<true, false, SH><<<blocks, NT, 0, stream>>>(G);
+    else if (!ta && tb) dgemm_group_kernel<false, true, SH><<<blocks, NT, 0, stream>>>(G);
+    else dgemm_group_kernel<true, true, SH><<<blocks, NT, 0, stream>>>(G);
 }
 
 // Deterministic split-K reduction: fixed summation order over the splits.
@@ -154,7 +240,7 @@ __global__ void dgemm_splitk_reduce(GemmArgs g) {
         const int64_t i = e % g.m, j = e / g.m;
         double s = 0.0;
         for (int z = 0; z < g.splitk; ++z) s += g.partial[((int64_t)z * g.batch + b) * mn + e];
-        double* c = g.C + i * g.rsC + j * g.csC + b * g.bsC;
+        double* c = g.C + c_row_offset(g, i) + j * g.csC + b * g.bsC;
         double v = g.alpha * s;
         if (g.beta != 0.0) v = fma(g.beta, *c, v);
         *c = v;
@@ -167,7 +253,7 @@ __global__ void scale_kernel(GemmArgs g) {
     for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
          idx += (int64_t)gridDim.x * blockDim.x) {
         const int64_t b = idx / mn, e = idx % mn;
-        double* c = g.C + (e % g.m) * g.rsC + (e / g.m) * g.csC + b * g.bsC;
+        double* c = g.C + c_row_offset(g, e % g.m) + (e / g.m) * g.csC + b * g.bsC;
         *c = g.beta == 0.0 ? 0.0 : g.beta * *c;
     }
 }
@@ -182,8 +268,10 @@ rt_status gemm_f64(const GemmF64& q, cudaStream_t stream) {
     g.m = q.m; g.n = q.n; g.k = q.k; g.alpha = q.alpha; g.beta = q.beta;
     g.A = q.A; g.lda = q.lda; g.sA = q.sA; g.B = q.B; g.ldb = q.ldb; g.sB = q.sB;
     g.C = q.C; g.rsC = q.rsC; g.csC = q.csC; g.bsC = q.bsC; g.batch = q.batch;
-    g.tiles_m = ceil_div(q.m, BM);
-    g.tiles_n = ceil_div(q.n, BN);
+    g.a_div = q.a_div; g.a_s1 = q.a_s1; g.c_md = q.c_md; g.c_ms1 = q.c_ms1;
+    const int shape = pick_shape(q.m, q.n);
+    g.tiles_m = ceil_div(q.m, (int64_t)tile_bm(shape));
+    g.tiles_n = ceil_div(q.n, (int64_t)tile_bn(shape));
     if (q.k == 0) {
         scale_kernel<<<1024, 256, 0, stream>>>(g);
         return check_launch("gemm_f64 scale");
@@ -201,10 +289,13 @@ rt_status gemm_f64(const GemmF64& q, cudaStream_t stream) {
     dim3 grid((unsigned)(g.tiles_m * g.tiles_n), (unsigned)(q.batch < 65535 ? q.batch : 65535), (unsigned)splitk);
     const bool ta = q.opa == 'T', tb = q.opb == 'T';
     prof_begin(PROF_DGEMM, stream);
-    if (!ta && !tb) dgemm_tile_kernel<false, false><<<grid, NT, 0, stream>>>(g);
-    else if (ta && !tb) dgemm_tile_kernel<true, false><<<grid, NT, 0, stream>>>(g);
-    else if (!ta && tb) dgemm_tile_kernel<false, true><<<grid, NT, 0, stream>>>(g);
-    else dgemm_tile_kernel<true, true><<<grid, NT, 0, stream>>>(g);
+    switch (shape) {
+        case 1: launch_tile<1>(ta, tb, grid, g, stream); break;
+        case 2: launch_tile<2>(ta, tb, grid, g, stream); break;
+        case 3: launch_tile<3>(ta, tb, grid, g, stream); break;
+        case 4: launch_tile<4>(ta, tb, grid, g, stream); break;
+        default: launch_tile<0>(ta, tb, grid, g, stream); break;
+    }
     prof_end(PROF_DGEMM, stream, 2.0 * (double)q.m * (double)q.n * (double)q.k * (double)q.batch);
     RT_TRY(check_launch("dgemm_tile_kernel"));
     if (splitk > 1) {
@@ -215,51 +306,84 @@ rt_status gemm_f64(const GemmF64& q, cudaStream_t stream) {
 }
 
 rt_status gemm_f64_many(const GemmF64* qs, int n, cudaStream_t stream) {
-    // Group by op pair; each group goes out in launches of up to kMaxGroupF64 products.
+    // Group by op pair and tile shape; each group goes out in launches of up to
+    // kMaxGroupF64 products.
+    for (int i = 0; i < n; ++i)
+        RT_REQUIRE(qs[i].m >= 0 && qs[i].n >= 0 && qs[i].k > 0 && qs[i].batch >= 0, "gemm_f64_many: bad size");
+    std::deque<ScratchBuf> parts;  // split-K partials, released after the reductions (stream order)
     for (int op = 0; op < 4; ++op) {
         const bool ta = op & 1, tb = op & 2;
-        GroupF64 G;
-        G.n = 0;
-        G.prefix[0] = 0;
-        double flops = 0.0;
-        auto flush = [&]() -> rt_status {
-            if (G.n == 0) return RT_OK;
-            for (int i = G.n; i < kMaxGroupF64; ++i) G.prefix[i + 1] = G.prefix[G.n];
-            const int64_t blocks = G.prefix[G.n];
-            if (blocks > 0) {
-                RT_REQUIRE(blocks < (int64_t)INT32_MAX, "gemm_f64_many: too many tiles for one launch");
-                prof_begin(PROF_DGEMM, stream);
-                if (!ta && !tb) dgemm_group_kernel<false, false><<<(unsigned)blocks, NT, 0, stream>>>(G);
-                else if (ta && !tb) dgemm_group_kernel<true, false><<<(unsigned)blocks, NT, 0, stream>>>(G);
-                else if (!ta && tb) dgemm_group_kernel<false, true><<<(unsigned)blocks, NT, 0, stream>>>(G);
-                else dgemm_group_kernel<true, true><<<(unsigned)blocks, NT, 0, stream>>>(G);
-                prof_end(PROF_DGEMM, stream, flops);
-                RT_TRY(check_launch("dgemm_group_kernel"));
-            }
+        for (int shape = 0; shape < kShapes; ++shape) {
+            GroupF64 G;
             G.n = 0;
-            flops = 0.0;
-            return RT_OK;
-        };
-        for (int i = 0; i < n; ++i) {
-            const GemmF64& q = qs[i];
-            if ((q.opa == 'T') != ta || (q.opb == 'T') != tb) continue;
-            RT_REQUIRE(q.m >= 0 && q.n >= 0 && q.k >= 0 && q.batch >= 0, "gemm_f64_many: negative size");
-            if (q.m == 0 || q.n == 0 || q.batch == 0) continue;
-            GemmArgs& g = G.a[G.n];
-            g = GemmArgs{};
-            g.m = q.m; g.n = q.n; g.k = q.k; g.alpha = q.alpha; g.beta = q.beta;
-            g.A = q.A; g.lda = q.lda; g.sA = q.sA; g.B = q.B; g.ldb = q.ldb; g.sB = q.sB;
-            g.C = q.C; g.rsC = q.rsC; g.csC = q.csC; g.bsC = q.bsC; g.batch = q.batch;
-            g.tiles_m = ceil_div(q.m, BM);
-            g.tiles_n = ceil_div(q.n, BN);
-            g.splitk = 1;
-            g.kchunk = std::max<int64_t>(BK, ceil_div(q.k, BK) * BK);
-            G.prefix[G.n + 1] = G.prefix[G.n] + g.tiles_m * g.tiles_n * q.batch;
-            flops += 2.0 * (double)q.m * (double)q.n * (double)q.k * (double)q.batch;
-            ++G.n;
-            if (G.n == kMaxGroupF64) RT_TRY(flush());
+            G.prefix[0] = 0;
+            double flops = 0.0;
+            auto flush = [&]() -> rt_status {
+                if (G.n == 0) return RT_OK;
+                for (int i = G.n; i < kMaxGroupF64; ++i) G.prefix[i + 1] = G.prefix[G.n];
+                const int64_t blocks = G.prefix[G.n];
+                if (blocks > 0) {
+                    RT_REQUIRE(blocks < (int64_t)INT32_MAX, "gemm_f64_many: too many tiles for one launch");
+                    prof_begin(PROF_DGEMM, stream);
+                    switch (shape) {
+                        case 1: launch_group<1>(ta, tb, (unsigned)blocks, G, stream); break;
+                        case 2: launch_group<2>(ta, tb, (unsigned)blocks, G, stream); break;
+                        case 3: launch_group<3>(ta, tb, (unsigned)blocks, G, stream); break;
+                        case 4: launch_group<4>(ta, tb, (unsigned)blocks, G, stream); break;
+                        default: launch_group<0>(ta, tb, (unsigned)blocks, G, stream); break;
+                    }
+                    prof_end(PROF_DGEMM, stream, flops);
+                    RT_TRY(check_launch("dgemm_group_kernel"));
+                    // One deterministic reduction for every split product of the launch.
+                    GroupF64 R;
+                    R.n = 0;
+                    R.prefix[0] = 0;
+                    for (int i = 0; i < G.n; ++i) {
+                        if (G.a[i].splitk <= 1) continue;
+                        R.a[R.n] = G.a[i];
+                        R.prefix[R.n + 1] = R.prefix[R.n] + G.a[i].m * G.a[i].n * G.a[i].batch;
+                        ++R.n;
+                    }
+                    if (R.n > 0) {
+                        for (int i = R.n; i < kMaxGroupF64; ++i) R.prefix[i + 1] = R.prefix[R.n];
+                        dgemm_splitk_reduce_group<<<2 * sm_count(), 256, 0, stream>>>(R);
+                        RT_TRY(check_launch("dgemm_splitk_reduce_group"));
+                    }
+                }
+                G.n = 0;
+                flops = 0.0;
+                return RT_OK;
+            };
+            for (int i = 0; i < n; ++i) {
+                const GemmF64& q = qs[i];
+                if ((q.opa == 'T') != ta || (q.opb == 'T') != tb) continue;
+                if (q.m == 0 || q.n == 0 || q.batch == 0) continue;
+                if (pick_shape(q.m, q.n) != shape) continue;
+                GemmArgs& g = G.a[G.n];
+                g = GemmArgs{};
+                g.m = q.m; g.n = q.n; g.k = q.k; g.alpha = q.alpha; g.beta = q.beta;
+                g.A = q.A; g.lda = q.lda; g.sA = q.sA; g.B = q.B; g.ldb = q.ldb; g.sB = q.sB;
+                g.C = q.C; g.rsC = q.rsC; g.csC = q.csC; g.bsC = q.bsC; g.batch = q.batch;
+                g.a_div = q.a_div; g.a_s1 = q.a_s1; g.c_md = q.c_md; g.c_ms1 = q.c_ms1;
+    g.a_div = q.a_div; g.a_s1 = q.a_s1; g.c_md = q.c_md; g.c_ms1 = q.c_ms1;
+                g.tiles_m = ceil_div(q.m, (int64_t)tile_bm(shape));
+                g.tiles_n = ceil_div(q.n, (int64_t)tile_bn(shape));
+                const int want = q.splitk < 1 ? 1 : q.splitk;
+                g.kchunk = std::max<int64_t>(BK, ceil_div(ceil_div(q.k, want), BK) * BK);
+                g.splitk = (int)std::max<int64_t>(1, ceil_div(q.k, g.kchunk));
+                if (g.splitk > 1) {
+                    parts.emplace_back();
+                    RT_TRY(scratch_alloc(parts.back(),
+                                         sizeof(double) * (size_t)g.splitk * q.batch * q.m * q.n, stream));
+                    g.partial = parts.back().as<double>();
+                }
+                G.prefix[G.n + 1] = G.prefix[G.n] + g.tiles_m * g.tiles_n * q.batch * g.splitk;
+                flops += 2.0 * (double)q.m * (double)q.n * (double)q.k * (double)q.batch;
+                ++G.n;
+                if (G.n == kMaxGroupF64) RT_TRY(flush());
+            }
+            RT_TRY(flush());
         }
-        RT_TRY(flush());
     }
     return RT_OK;
 }
@@ -556,8 +680,10 @@ rt_status launch_dgemm_noalloc(const GemmF64& q, cudaStream_t stream) {
     g.m = q.m; g.n = q.n; g.k = q.k; g.alpha = q.alpha; g.beta = q.beta;
     g.A = q.A; g.lda = q.lda; g.sA = q.sA; g.B = q.B; g.ldb = q.ldb; g.sB = q.sB;
     g.C = q.C; g.rsC = q.rsC; g.csC = q.csC; g.bsC = q.bsC; g.batch = q.batch;
-    g.tiles_m = ceil_div(q.m, BM);
-    g.tiles_n = ceil_div(q.n, BN);
+    g.a_div = q.a_div; g.a_s1 = q.a_s1; g.c_md = q.c_md; g.c_ms1 = q.c_ms1;
+    const int shape = pick_shape(q.m, q.n);
+    g.tiles_m = ceil_div(q.m, (int64_t)tile_bm(shape));
+    g.tiles_n = ceil_div(q.n, (int64_t)tile_bn(shape));
     g.splitk = 1;
     g.kchunk = ceil_div(std::max<int64_t>(q.k, 1), BK) * BK;
     if (q.k == 0) {
@@ -566,10 +692,13 @@ rt_status launch_dgemm_noalloc(const GemmF64& q, cudaStream_t stream) {
     }
     dim3 grid((unsigned)(g.tiles_m * g.tiles_n), (unsigned)(q.batch < 65535 ? q.batch : 65535), 1u);
     const bool ta = q.opa == 'T', tb = q.opb == 'T';
-    if (!ta && !tb) dgemm_tile_kernel<false, false><<<grid, NT, 0, stream>>>(g);
-    else if (ta && !tb) dgemm_tile_kernel<true, false><<<grid, NT, 0, stream>>>(g);
-    else if (!ta && tb) dgemm_tile_kernel<false, true><<<grid, NT, 0, stream>>>(g);
-    else dgemm_tile_kernel<true, true><<<grid, NT, 0, stream>>>(g);
+    switch (shape) {
+        case 1: launch_tile<1>(ta, tb, grid, g, stream); break;
+        case 2: launch_tile<2>(ta, tb, grid, g, stream); break;
+        case 3: launch_tile<3>(ta, tb, grid, g, stream); break;
+        case 4: launch_tile<4>(ta, tb, grid, g, stream); break;
+        default: launch_tile<0>(ta, tb, grid, g, stream); break;
+    }
     return check_launch("dgemm_tile_kernel");
 }
 

@@ -86,6 +86,9 @@ int sm_count();
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
+// "No composite index": a divisor larger than any row count.
+constexpr int64_t kNoDiv = (int64_t)1 << 62;
+
 // FP64 GEMM service used by every plain-form contraction.  Column-major.
 //   C_b(i,j) = alpha * sum_k opA(A_b)(i,k) opB(B_b)(k,j) + beta * C_b(i,j)
 //   A_b = A + b*sA, B_b = B + b*sB,
@@ -102,10 +105,15 @@ struct GemmF64 {
     int64_t rsC = 1, csC = 0, bsC = 0;
     int64_t batch = 1;
     int splitk = 1;  // >1: partial sums in scratch, reduced deterministically
+    // Composite row index (rows that are a pair (r % div, r / div)):
+    //   A row r at (r % a_div) + (r / a_div) * a_s1 (opa 'N'; times lda for 'T'),
+    //   C row r at (r % c_md) * rsC + (r / c_md) * c_ms1.
+    int64_t a_div = kNoDiv, a_s1 = 0;
+    int64_t c_md = kNoDiv, c_ms1 = 0;
 };
 rt_status gemm_f64(const GemmF64& g, cudaStream_t stream);
-// Several float64 GEMMs in one launch per op pair (no split-K; k == 0 is not
-// accepted here).
+// Several float64 GEMMs in one launch per op pair and tile shape (k == 0 is
+// not accepted here); products with splitk > 1 share one reduction launch.
 rt_status gemm_f64_many(const GemmF64* gs, int n, cudaStream_t stream);
 
 // Split-precision (BF16 digit planes on tcgen05, exact integer
@@ -115,7 +123,6 @@ rt_status gemm_f64_many(const GemmF64* gs, int n, cudaStream_t stream);
 // Each operand needs unit stride along k (sk == 1) or along rows (s0 == 1).
 // nslices in [3, 8].  b_is_a reuses A's digit planes for B; symmetric (with
 // b_is_a) computes only n >= m and mirrors.
-constexpr int64_t kNoDiv = (int64_t)1 << 62;
 struct OzOperand {
     const double* p = nullptr;
     int64_t rows = 0, div = kNoDiv, s0 = 0, s1 = 0, sk = 1;

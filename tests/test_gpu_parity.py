@@ -53,8 +53,12 @@ def test_gemm_seam_doctests_on_gpu(name):
     assert m[r0:r1, c0:c1].flatten(order="F").tolist() == c["expected"]
 
 
+# Shapes cover every float64 tile form: 64x64, 128x32 (n <= 32), 32x128 (m <= 32),
+# 256x16 (n <= 16) and 16x256 (m <= 16), under all four op pairs.
 @pytest.mark.parametrize("opa,opb,m,n,k", [("N", "N", 70, 33, 129), ("T", "N", 64, 64, 17), ("N", "T", 1, 200, 5),
-                                           ("T", "T", 129, 65, 300), ("N", "N", 40, 30, 5000)])
+                                           ("T", "T", 129, 65, 300), ("N", "N", 40, 30, 5000),
+                                           ("T", "N", 20, 100, 50), ("N", "T", 300, 7, 90), ("T", "T", 9, 333, 77),
+                                           ("N", "N", 257, 16, 33), ("T", "N", 100, 31, 64), ("N", "T", 31, 97, 19)])
 def test_rt_dgemm_matches_oracle(opa, opb, m, n, k):
     rng = np.random.default_rng(m * 7 + n)
     A = np.asfortranarray(rng.standard_normal((m, k) if opa == "N" else (k, m)))
