@@ -246,26 +246,30 @@ __global__ void __launch_bounds__(256) slice_strided_kernel(SliceArgs a) {
     }
 }
 
-// Strided rows (s0 == 1) with a short contraction (K <= 128 * NBLK): row
-// exponents and digits in one pass.  A CTA covers 16 rows and all of k; each
-// thread keeps its NBLK runs of 8 consecutive k in registers, the 16 threads of
-// a row reduce its exponent maximum, then every thread slices its runs.
-// Replaces emax_strided_kernel + slice_strided_kernel (one read of the operand
-// instead of two); rows beyond the operand (tile padding) get zero digits.
-constexpr int kFusedRows = 16;
-template <int S, int NBLK>
-__global__ void __launch_bounds__(256, 2) slice_strided_rowmax_kernel(SliceArgs a, int* __restrict__ emax_out) {
-    __shared__ unsigned int red[8][kFusedRows];
-    const int r = threadIdx.x & (kFusedRows - 1);
-    const int kq = threadIdx.x >> 4;  // 0..15
-    const int64_t row = (int64_t)blockIdx.x * kFusedRows + r;
+// Strided rows (s0 == 1) with a short contraction (K <= 8 * (256 / RR) * NBLK):
+// row exponents and digits in one pass.  A CTA covers RR rows and all of k;
+// thread t takes row t % RR and k-groups t / RR + (256 / RR) j of 8 consecutive
+// k, kept in registers.  The threads of a row reduce its exponent maximum
+// (shuffles inside a warp, then 8 shared words), then every thread slices its
+// runs.  Replaces emax_strided_kernel + slice_strided_kernel (one read of the
+// operand instead of two); rows beyond the operand (tile padding) get zero digits.
+constexpr int kFusedRows = 16;    // contiguous-row slicer
+constexpr int kStridedRows = 16;  // strided-row slicer (8 rows at 3 CTAs/SM measured slower)
+template <int S, int NBLK, int RR>
+__global__ void __launch_bounds__(256, RR >= 16 ? 2 : 3)
+    slice_strided_rowmax_kernel(SliceArgs a, int* __restrict__ emax_out) {
+    constexpr int KQN = 256 / RR;
+    __shared__ unsigned int red[8][RR];
+    const int r = threadIdx.x % RR;
+    const int kq = threadIdx.x / RR;
+    const int64_t row = (int64_t)blockIdx.x * RR + r;
     const bool valid = row < a.src.rows;
     const double* base = valid ? a.src.p + (row % a.src.div) * a.src.s0 + (row / a.src.div) * a.src.s1 : nullptr;
     double x[NBLK][8];
     unsigned int m = 0;
 #pragma unroll
     for (int j = 0; j < NBLK; ++j) {
-        const int64_t k0 = (int64_t)(kq + 16 * j) * 8;
+        const int64_t k0 = (int64_t)(kq + KQN * j) * 8;
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
             const int64_t k = k0 + i;
@@ -273,9 +277,10 @@ __global__ void __launch_bounds__(256, 2) slice_strided_rowmax_kernel(SliceArgs 
             m = max(m, ((unsigned int)__double2hiint(x[j][i]) >> 20) & 0x7FFu);
         }
     }
-    // threads r and r + 16 of a warp share the row; then across the 8 warps
-    m = max(m, __shfl_xor_sync(0xffffffffu, m, 16));
-    if ((threadIdx.x & 31) < kFusedRows) red[threadIdx.x >> 5][r] = m;
+    // lanes r, r + RR, ... of a warp share the row; then across the 8 warps
+#pragma unroll
+    for (int o = RR; o < 32; o <<= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) < RR) red[threadIdx.x >> 5][r] = m;
     __syncthreads();
 #pragma unroll
     for (int w = 0; w < 8; ++w) m = max(m, red[w][r]);
@@ -287,7 +292,7 @@ __global__ void __launch_bounds__(256, 2) slice_strided_rowmax_kernel(SliceArgs 
     const int rt_ = (int)(row % a.T);
 #pragma unroll
     for (int j = 0; j < NBLK; ++j) {
-        const int64_t k0 = (int64_t)(kq + 16 * j) * 8;
+        const int64_t k0 = (int64_t)(kq + KQN * j) * 8;
         if (k0 >= a.Kb * KB) continue;
         uint32_t w[S][4];
         digits8<S>(x[j], (int)m, w);
@@ -886,14 +891,16 @@ rt_status slice_operand(const Operand& op, int64_t K, int T, Sliced& out, cudaSt
         dim3 grid((unsigned)out.tiles, (unsigned)ceil_div(K, SK));
         slice_contig_kernel<S><<<grid, 256, 0, stream>>>(sa);
         RT_TRY(check_launch("slice_contig_kernel"));
-    } else if (op.s0 == 1 && out.Kb * KB <= 128 * 5) {
-        const unsigned grid = (unsigned)(out.tiles * T / kFusedRows);
-        switch ((int)ceil_div(out.Kb, 8)) {
-            case 1: slice_strided_rowmax_kernel<S, 1><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
-            case 2: slice_strided_rowmax_kernel<S, 2><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
-            case 3: slice_strided_rowmax_kernel<S, 3><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
-            case 4: slice_strided_rowmax_kernel<S, 4><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
-            default: slice_strided_rowmax_kernel<S, 5><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
+    } else if (op.s0 == 1 && out.Kb * KB <= 640) {
+        constexpr int RR = kStridedRows, KQN = 256 / RR;
+        const unsigned grid = (unsigned)(out.tiles * T / RR);
+        switch ((int)ceil_div(out.Kb * KB, 8 * KQN)) {
+            case 1: slice_strided_rowmax_kernel<S, 1, RR><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
+            case 2: slice_strided_rowmax_kernel<S, 2, RR><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
+            case 3: slice_strided_rowmax_kernel<S, 3, RR><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
+            case 4: slice_strided_rowmax_kernel<S, 4, RR><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
+            default: slice_strided_rowmax_kernel<S, (640 + 8 * KQN - 1) / (8 * KQN), RR>
+                         <<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
         }
         RT_TRY(check_launch("slice_strided_rowmax_kernel"));
     } else if (op.s0 == 1) {
