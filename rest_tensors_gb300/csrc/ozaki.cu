@@ -142,14 +142,6 @@ __device__ __forceinline__ void split_digits(double x, int emax, int (&d)[S]) {
     }
 }
 
-// Exact BF16 bit pattern of a small integer (|v| <= 256).  The float with bits
-// 0x4B400000 + v is 1.5 * 2^23 + v (for |v| < 2^22), so one FP32 subtraction
-// gives v exactly, without the int-to-float conversion pipe; v has at most 8
-// significant bits, so its BF16 pattern is the float's upper half.
-__device__ __forceinline__ uint32_t bf16_of_int(int v) {
-    const float f = __int_as_float(0x4B400000 + v) - 12582912.0f;
-    return __float_as_uint(f) >> 16;
-}
 
 // -------------------------------------------------------------- row scale --
 
@@ -194,18 +186,49 @@ __global__ void emax_strided_kernel(Operand a, int64_t K, int64_t kspan, int* __
 // --------------------------------------------------------------- slicing --
 
 // Pack the S digit planes of 8 consecutive k of one row into 16-byte words.
+// The same digits as exact floats, at three operations per digit: a funnel
+// shift brings the 7-bit field (the digit + 64) to the low bits, one LOP3 masks
+// it and inserts the exponent of 2^23 (the float 2^23 + u), and one FMA by +-1
+// removes 2^23 + 64 and applies x's sign.  (split_digits states the digits
+// with integer arithmetic; both give the same values.)
+template <int S>
+__device__ __forceinline__ void split_digits_f(double x, int emax, float (&f)[S]) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((bits >> 52) & 0x7FF);
+    const int sh = emax - e + 1;
+    if (e == 0 || sh >= 64) {
+#pragma unroll
+        for (int s = 0; s < S; ++s) f[s] = 0.0f;
+        return;
+    }
+    const unsigned long long full = ((bits & 0xFFFFFFFFFFFFFull) | (1ull << 52)) << 10;
+    unsigned long long q = full >> sh;
+    q |= (full & ((1ull << sh) - 1ull)) != 0ull ? 1ull : 0ull;
+    constexpr int L = DigitConst<S>::L;
+    const unsigned long long t = q + ((1ull << (L - 1)) - 1ull) + ((q >> L) & 1ull) + DigitConst<S>::off();
+    const uint32_t hi = (uint32_t)(t >> 32), lo = (uint32_t)t;
+    const float sg = (bits >> 63) ? -1.0f : 1.0f;
+    // leading digit: t >> 56, no bias
+    f[0] = __fmaf_rn(__uint_as_float((hi >> 24) | 0x4B000000u), sg, -8388608.0f * sg);
+    const float c = -8388672.0f * sg;  // -(2^23 + 64) * sign
+#pragma unroll
+    for (int s = 1; s < S; ++s) {
+        const int pos = 56 - 7 * s;
+        const uint32_t win = pos >= 32 ? (hi >> (pos - 32)) : __funnelshift_r(lo, hi, pos);
+        f[s] = __fmaf_rn(__uint_as_float((win & 127u) | 0x4B000000u), sg, c);
+    }
+}
+
 template <int S>
 __device__ __forceinline__ void digits8(const double (&x)[8], int em, uint32_t (&w)[S][4]) {
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-        int d[S];
-        split_digits<S>(x[j], em, d);
+    for (int jp = 0; jp < 4; ++jp) {
+        float f0[S], f1[S];
+        split_digits_f<S>(x[2 * jp], em, f0);
+        split_digits_f<S>(x[2 * jp + 1], em, f1);
+        // BF16 patterns are the floats' upper halves (the digits have <= 8 significant bits)
 #pragma unroll
-        for (int s = 0; s < S; ++s) {
-            const uint32_t h = bf16_of_int(d[s]);
-            if (j & 1) w[s][j >> 1] |= h << 16;
-            else w[s][j >> 1] = h;
-        }
+        for (int s = 0; s < S; ++s) w[s][jp] = __byte_perm(__float_as_uint(f0[s]), __float_as_uint(f1[s]), 0x7632u);
     }
 }
 
