@@ -232,6 +232,9 @@ rt_status rt_ri_ov_k(const double* C, const double* B, int nb, int naux, int noc
     return ri_ov_k_split(C, B, nb, naux, nocc, nvir, ov, K, nslices, s);
 }
 
+// Digit-plane bytes one grouped split launch of the batched entry may hold.
+constexpr size_t kBatchPlaneBytes = (size_t)24 << 30;
+
 rt_status rt_ri_ov_k_batched(const rt_ri_problem* probs, int nprob, int form, int nslices, const rt_tuning* tuning,
                              void* stream) {
     RT_REQUIRE(nprob >= 0 && (nprob == 0 || probs), "rt_ri_ov_k_batched: bad problem list");
@@ -331,9 +334,26 @@ rt_status rt_ri_ov_k_batched(const rt_ri_problem* probs, int nprob, int form, in
             g3.push_back(c);
         }
     }
-    RT_TRY(oz_gemm_many(g1.data(), (int)g1.size(), s));
-    RT_TRY(oz_gemm_many(g2.data(), (int)g2.size(), s));
-    RT_TRY(oz_gemm_many(g3.data(), (int)g3.size(), s));
+    // Each grouped launch holds the digit planes of all its products at once:
+    // flush in sub-batches of at most kBatchPlaneBytes of planes.
+    auto run = [&](std::vector<OzGemm>& gs) -> rt_status {
+        size_t i0 = 0, bytes = 0;
+        for (size_t i = 0; i < gs.size(); ++i) {
+            const OzGemm& g = gs[i];
+            const size_t b = (size_t)(g.A.rows + (g.b_is_a ? 0 : g.B.rows)) * (size_t)g.K * 2u * (size_t)nslices;
+            if (i > i0 && bytes + b > kBatchPlaneBytes) {
+                RT_TRY(oz_gemm_many(gs.data() + i0, (int)(i - i0), s));
+                i0 = i;
+                bytes = 0;
+            }
+            bytes += b;
+        }
+        if (i0 < gs.size()) RT_TRY(oz_gemm_many(gs.data() + i0, (int)(gs.size() - i0), s));
+        return RT_OK;
+    };
+    RT_TRY(run(g1));
+    RT_TRY(run(g2));
+    RT_TRY(run(g3));
     return RT_OK;
 }
 
