@@ -251,6 +251,17 @@ void rt_profile_enable(int on);
  * (synchronises the recorded events). */
 rt_status rt_profile_get(int kind, double* total_ms, long long* launches, double* work);
 
+/* ---- Testing hooks (no counterpart in the reference) ----
+ * rt_debug_fail_alloc_after(n): the next n scratch allocations succeed and the
+ * one after fails with RT_ERR_NO_MEMORY (n < 0: off).  Process-wide.
+ * rt_debug_wait_timeout(cycles, stream): a one-thread kernel waits on a barrier
+ * that nothing arrives at, for at most `cycles` clock cycles (<= 2e9), then sets
+ * the device error word's timeout flag and returns normally; rt_sync_status()
+ * then reports RT_ERR_TIMEOUT.  This is the library's bounded-wait path run out
+ * on purpose; no device fault is raised. */
+rt_status rt_debug_fail_alloc_after(long long n);
+rt_status rt_debug_wait_timeout(long long cycles, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -124,6 +124,10 @@ def lib() -> ctypes.CDLL:
     L.rt_davidson_ri_response.argtypes = [vp, vp, ctypes.c_longlong, c_int, c_int, c_int, vp,
                                           ctypes.POINTER(_DavidsonParamsC), c_int, ctypes.POINTER(c_int),
                                           ctypes.POINTER(c_dbl), vp, ctypes.POINTER(c_int), vp]
+    L.rt_debug_fail_alloc_after.restype = c_int
+    L.rt_debug_fail_alloc_after.argtypes = [ctypes.c_longlong]
+    L.rt_debug_wait_timeout.restype = c_int
+    L.rt_debug_wait_timeout.argtypes = [ctypes.c_longlong, vp]
     L.ri_ao2mo_f_.restype = None
     L.general_dgemm_f_.restype = None
     _lib = L
@@ -533,6 +537,16 @@ def davidson_ri_response(Bov, delta, nov: int, naux: int, x0_1d, params: Davidso
                                          ctypes.byref(pc), print_level, conv, e, _dptr(x), ctypes.byref(its),
                                          _stream(stream)))
     return [bool(c) for c in conv], list(e), x.view(nr, nov), its.value
+
+
+def debug_fail_alloc_after(n: int) -> None:
+    """Testing hook: the next n scratch allocations succeed, the one after fails (n < 0: off)."""
+    _check(lib().rt_debug_fail_alloc_after(n))
+
+
+def debug_wait_timeout(cycles: int, stream=None) -> None:
+    """Testing hook: run the bounded-wait path out on purpose (see rt_debug_wait_timeout)."""
+    _check(lib().rt_debug_wait_timeout(cycles, _stream(stream)))
 
 
 def sync_status(stream=None) -> None:

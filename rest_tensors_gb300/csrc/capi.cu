@@ -1,6 +1,7 @@
 // capi.cu - the exported C ABI: the reference's Fortran seam (drop-in, host
 // pointers) and the rt_* device-pointer API, composed from the float64 and
 // split-precision GEMM services.
+#include <nvtx3/nvToolsExt.h>
 #include <string.h>
 
 #include <algorithm>
@@ -9,6 +10,15 @@
 #include "rt_internal.cuh"
 
 namespace rt {
+
+// NVTX range over one entry point (visible in Nsight timelines; no cost without a tool).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
+
 
 rt_status ri_j_fp64(const double* B, const double* D, int nb, int naux, double* w, double* J, cudaStream_t stream);
 rt_status exchange_energy(const double* D, const double* K, int nb, double* out, cudaStream_t stream);
@@ -157,6 +167,7 @@ extern "C" {
 
 rt_status rt_dgemm(char opa, char opb, int m, int n, int k, double alpha, const double* A, int lda, const double* B,
                    int ldb, double beta, double* C, int ldc, void* stream) {
+    NvtxRange nvtx_range("rt_dgemm");
     RT_REQUIRE(m >= 0 && n >= 0 && k >= 0, "rt_dgemm: negative dimension");
     RT_REQUIRE(opa == 'N' || opa == 'T' || opa == 'n' || opa == 't', "rt_dgemm: opa must be N or T");
     RT_REQUIRE(opb == 'N' || opb == 'T' || opb == 'n' || opb == 't', "rt_dgemm: opb must be N or T");
@@ -175,6 +186,7 @@ rt_status rt_dgemm(char opa, char opb, int m, int n, int k, double alpha, const 
 
 rt_status rt_dgemm_split(char opa, char opb, int m, int n, int k, const double* A, int lda, const double* B, int ldb,
                          double* C, int ldc, int nslices, void* stream) {
+    NvtxRange nvtx_range("rt_dgemm_split");
     RT_REQUIRE(m >= 0 && n >= 0 && k >= 0, "rt_dgemm_split: negative dimension");
     RT_REQUIRE(opa == 'N' || opa == 'T', "rt_dgemm_split: opa must be N or T");
     RT_REQUIRE(opb == 'N' || opb == 'T', "rt_dgemm_split: opb must be N or T");
@@ -208,6 +220,7 @@ rt_status rt_dgemm_split(char opa, char opb, int m, int n, int k, const double* 
 
 rt_status rt_ri_ao2mo(const double* C, const double* B, double* ri3mo, int nb, int ns, int naux, int form,
                       int nslices, void* stream) {
+    NvtxRange nvtx_range("rt_ri_ao2mo");
     RT_REQUIRE(nb >= 0 && ns >= 0 && naux >= 0, "rt_ri_ao2mo: negative dimension");
     RT_REQUIRE(valid_form(form, nslices), "rt_ri_ao2mo: bad form/nslices (%d, %d)", form, nslices);
     if ((int64_t)nb * ns * naux == 0) return RT_OK;
@@ -218,6 +231,7 @@ rt_status rt_ri_ao2mo(const double* C, const double* B, double* ri3mo, int nb, i
 
 rt_status rt_ri_ov_k(const double* C, const double* B, int nb, int naux, int nocc, int nvir, double* ov, double* K,
                      int form, int nslices, void* stream) {
+    NvtxRange nvtx_range("rt_ri_ov_k");
     RT_REQUIRE(nb >= 0 && naux >= 0 && nocc >= 0 && nvir >= 0, "rt_ri_ov_k: negative dimension");
     RT_REQUIRE(valid_form(form, nslices), "rt_ri_ov_k: bad form/nslices (%d, %d)", form, nslices);
     cudaStream_t s = (cudaStream_t)stream;
@@ -237,6 +251,7 @@ constexpr size_t kBatchPlaneBytes = (size_t)24 << 30;
 
 rt_status rt_ri_ov_k_batched(const rt_ri_problem* probs, int nprob, int form, int nslices, const rt_tuning* tuning,
                              void* stream) {
+    NvtxRange nvtx_range("rt_ri_ov_k_batched");
     RT_REQUIRE(nprob >= 0 && (nprob == 0 || probs), "rt_ri_ov_k_batched: bad problem list");
     RT_REQUIRE(valid_form(form, nslices), "rt_ri_ov_k_batched: bad form/nslices (%d, %d)", form, nslices);
     cudaStream_t s = (cudaStream_t)stream;
@@ -358,6 +373,7 @@ rt_status rt_ri_ov_k_batched(const rt_ri_problem* probs, int nprob, int form, in
 }
 
 rt_status rt_ri_j(const double* B, const double* D, int nb, int naux, double* w, double* J, void* stream) {
+    NvtxRange nvtx_range("rt_ri_j");
     RT_REQUIRE(nb >= 0 && naux >= 0, "rt_ri_j: negative dimension");
     cudaStream_t s = (cudaStream_t)stream;
     if (naux == 0) {
@@ -373,6 +389,7 @@ rt_status rt_ri_j(const double* B, const double* D, int nb, int naux, double* w,
 }
 
 rt_status rt_ri_exchange_energy(const double* D, const double* K, int nb, double* ex_device, void* stream) {
+    NvtxRange nvtx_range("rt_ri_exchange_energy");
     RT_REQUIRE(nb >= 0 && ex_device, "rt_ri_exchange_energy: bad argument");
     return exchange_energy(D, K, nb, ex_device, (cudaStream_t)stream);
 }
@@ -394,6 +411,7 @@ rt_status rt_synth_coef_seed(uint64_t seed, int nb, double* M, void* stream) {
 
 rt_status rt_ri_ov_k_host(const double* C, const double* B, int nb, int naux, int nocc, int nvir, double* ov,
                           double* K, int form, int nslices, void* stream) {
+    NvtxRange nvtx_range("rt_ri_ov_k_host");
     RT_REQUIRE(nb >= 0 && naux >= 0 && nocc >= 0 && nvir >= 0, "rt_ri_ov_k_host: negative dimension");
     RT_REQUIRE(valid_form(form, nslices), "rt_ri_ov_k_host: bad form/nslices");
     cudaStream_t s = (cudaStream_t)stream;
@@ -487,6 +505,7 @@ rt_status rt_ri_ov_k_host(const double* C, const double* B, int nb, int naux, in
 
 void ri_ao2mo_f_(const double* eigenvector, const double* ri3fn, double* ri3mo, const int* num_states,
                  const int* num_basis, const int* num_auxbas) {
+    NvtxRange nvtx_range("ri_ao2mo_f_");
     rt::set_error(RT_OK, "");
     const int ns = *num_states, nb = *num_basis, naux = *num_auxbas;
     const size_t nR = (size_t)naux * ns * ns;
@@ -519,6 +538,7 @@ void general_dgemm_f_(const double* matr_a, const int* rows_a, const int* column
                       double* matr_c, const int* rows_c, const int* columns_c, const int* start_row_c,
                       const int* len_row_c, const int* start_column_c, const int* len_column_c,
                       const double* alpha, const double* beta) {
+    NvtxRange nvtx_range("general_dgemm_f_");
     rt::set_error(RT_OK, "");
     auto run = [&]() -> rt_status {
         const char oa = *opa, ob = *opb;

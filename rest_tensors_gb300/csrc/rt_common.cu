@@ -182,7 +182,20 @@ rt_status rt_sync_status(void* stream) {
 
 namespace rt {
 
+// Fault-injection hook for tests: when >= 0, the count of scratch allocations
+// that still succeed; the next one fails with RT_ERR_NO_MEMORY.
+static std::atomic<long long> g_fail_alloc_after{-1};
+
 rt_status scratch_alloc(ScratchBuf& b, size_t bytes, cudaStream_t stream) {
+    long long left = g_fail_alloc_after.load(std::memory_order_relaxed);
+    while (left >= 0 && !g_fail_alloc_after.compare_exchange_weak(left, left - 1)) {
+    }
+    if (left == 0) {
+        b.p = nullptr;
+        set_error(RT_ERR_NO_MEMORY, "scratch allocation of %zu bytes failed: injected by rt_debug_fail_alloc_after",
+                  bytes);
+        return RT_ERR_NO_MEMORY;
+    }
     static std::once_flag once;
     std::call_once(once, [] {
         // Keep freed pool memory mapped between calls so repeated calls do
@@ -208,3 +221,45 @@ rt_status scratch_alloc(ScratchBuf& b, size_t bytes, cudaStream_t stream) {
 }
 
 }  // namespace rt
+
+namespace {
+
+// One thread waits on an mbarrier that nothing arrives at, for at most
+// `cycles` clock cycles, then records DEV_ERR_TIMEOUT and returns: the same
+// bounded wait every pipeline of this library uses, run out on purpose.
+__global__ void wait_timeout_kernel(long long cycles, unsigned int* err) {
+    __shared__ uint64_t bar;
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(&bar);
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(a) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    const long long t0 = clock64();
+    while (true) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], 0;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(a)
+            : "memory");
+        if (ok) return;  // cannot happen: nothing arrives
+        if (clock64() - t0 > cycles) {
+            atomicOr(err, rt::DEV_ERR_TIMEOUT);
+            return;
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" rt_status rt_debug_fail_alloc_after(long long n) {
+    rt::g_fail_alloc_after.store(n < 0 ? -1 : n);
+    return RT_OK;
+}
+
+extern "C" rt_status rt_debug_wait_timeout(long long cycles, void* stream) {
+    RT_REQUIRE(cycles >= 0 && cycles <= 2000000000LL, "rt_debug_wait_timeout: cycles must be in [0, 2e9]");
+    unsigned int* err = rt::error_word_device();
+    RT_REQUIRE(err != nullptr, "rt_debug_wait_timeout: device error word unavailable");
+    wait_timeout_kernel<<<1, 1, 0, (cudaStream_t)stream>>>(cycles, err);
+    return rt::check_launch("wait_timeout_kernel");
+}
