@@ -236,6 +236,17 @@ rt_status rt_synth_coef_seed(uint64_t seed, int nb, double* M, void* stream);
 rt_status rt_ri_ov_k_host(const double* C, const double* B, int nb, int naux, int nocc, int nvir, double* ov,
                           double* K, int form, int nslices, void* stream);
 
+/* rt_ri_ov_k_host for symmetric ri3ao slabs (B^P_{mu,nu} = B^P_{nu,mu}, as the
+ * three-centre integrals (mu nu|P) always are): only the upper triangle of each
+ * slab crosses the host link and the lower triangle is mirrored on the device.
+ * Page-locked B is read in place by a gather kernel (2 CTAs per SM, on a
+ * high-priority stream); pageable B goes by 3-D copies of 32-column blocks.
+ * The results are those of rt_ri_ov_k_host on the slabs symmetrised from their
+ * upper triangles.  No counterpart in the reference (its ri_ao2mo_f reads the
+ * full tensor). */
+rt_status rt_ri_ov_k_host_symmetric(const double* C, const double* B, int nb, int naux, int nocc, int nvir,
+                                    double* ov, double* K, int form, int nslices, void* stream);
+
 /* ------------------------------------------------------------------------
  * Instrumentation.
  * ------------------------------------------------------------------------ */

@@ -97,6 +97,8 @@ def lib() -> ctypes.CDLL:
     L.rt_ri_ov_k_batched.argtypes = [ctypes.POINTER(RiProblem), c_int, c_int, c_int, ctypes.POINTER(Tuning), vp]
     L.rt_ri_ov_k_host.restype = c_int
     L.rt_ri_ov_k_host.argtypes = [vp, vp, c_int, c_int, c_int, c_int, vp, vp, c_int, c_int, vp]
+    L.rt_ri_ov_k_host_symmetric.restype = c_int
+    L.rt_ri_ov_k_host_symmetric.argtypes = [vp, vp, c_int, c_int, c_int, c_int, vp, vp, c_int, c_int, vp]
     L.rt_ri_j.restype = c_int
     L.rt_ri_j.argtypes = [vp, vp, c_int, c_int, vp, vp, vp]
     L.rt_ri_exchange_energy.restype = c_int
@@ -361,13 +363,17 @@ def ri_ov_k_batched(problems, form: str = "split", nslices: int = DEFAULT_NSLICE
 
 
 def ri_ov_k_host(C: np.ndarray, B: np.ndarray, nb: int, naux: int, nocc: int, nvir: int, ov: np.ndarray,
-                 K: np.ndarray, form: str = "split", nslices: int = DEFAULT_NSLICES, stream=None) -> None:
-    """Host-buffer form (numpy or pinned memory addresses): copies in, runs, copies out."""
+                 K: np.ndarray, form: str = "split", nslices: int = DEFAULT_NSLICES, stream=None,
+                 symmetric: bool = False) -> None:
+    """Host-buffer form (numpy or pinned memory addresses): copies in, runs, copies out.
+
+    symmetric=True reads only the upper triangle of each ri3ao slab from the host
+    (rt_ri_ov_k_host_symmetric); the slabs must be symmetric."""
     def hp(a):
         return a.ctypes.data if isinstance(a, np.ndarray) else int(a)
 
-    _check(lib().rt_ri_ov_k_host(hp(C), hp(B), nb, naux, nocc, nvir, hp(ov), hp(K), _form(form), nslices,
-                                 _stream(stream)))
+    fn = lib().rt_ri_ov_k_host_symmetric if symmetric else lib().rt_ri_ov_k_host
+    _check(fn(hp(C), hp(B), nb, naux, nocc, nvir, hp(ov), hp(K), _form(form), nslices, _stream(stream)))
 
 
 def ri_j(B, D, nb: int, naux: int, w=None, J=None, stream=None):

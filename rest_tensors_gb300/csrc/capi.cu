@@ -409,9 +409,118 @@ rt_status rt_synth_coef_seed(uint64_t seed, int nb, double* M, void* stream) {
     return synth_coef_seed(seed, nb, M, (cudaStream_t)stream);
 }
 
-rt_status rt_ri_ov_k_host(const double* C, const double* B, int nb, int naux, int nocc, int nvir, double* ov,
-                          double* K, int form, int nslices, void* stream) {
-    NvtxRange nvtx_range("rt_ri_ov_k_host");
+}  // extern "C"
+
+namespace rt {
+namespace {
+
+// Strict lower triangle of every [nb x nb] slab from its upper triangle:
+// block (tx, ty) of CTA (P, I >= J) reads the 32 x 32 tile of rows J, columns I
+// and writes its transpose to rows I, columns J through shared memory (in a
+// diagonal tile, only the elements below the diagonal).
+__global__ void __launch_bounds__(256) sym_mirror_kernel(double* __restrict__ B, int nb, int nbt, int64_t np) {
+    __shared__ double t[32][33];
+    const int64_t pairs = (int64_t)nbt * (nbt + 1) / 2;  // tiles on or below the diagonal
+    const int64_t idx = blockIdx.x;
+    const int64_t P = idx / pairs;
+    if (P >= np) return;
+    int64_t q = idx % pairs;
+    int I = 0;
+    while (q >= I + 1) {  // row-major enumeration of (I, J), J <= I
+        q -= I + 1;
+        ++I;
+    }
+    const int J = (int)q;
+    double* slab = B + P * (int64_t)nb * nb;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    // upper tile: rows mu = J*32 + tx, columns nu = I*32 + r  (mu < nu)
+    for (int r = ty; r < 32; r += 8) {
+        const int mu = J * 32 + tx, nu = I * 32 + r;
+        if (mu < nb && nu < nb) t[r][tx] = slab[mu + (int64_t)nb * nu];
+    }
+    __syncthreads();
+    // lower tile: rows nu = I*32 + tx, columns mu = J*32 + r
+    for (int r = ty; r < 32; r += 8) {
+        const int nu = I * 32 + tx, mu = J * 32 + r;
+        if (mu < nb && nu < nb && nu > mu) slab[nu + (int64_t)nb * mu] = t[tx][r];
+    }
+}
+
+// Zero-copy form for page-locked host memory: a small grid reads the upper
+// 32x32 tiles (I <= J; in a diagonal tile the upper half) of every slab straight
+// from host memory over the host link and writes each tile and its mirror to
+// device memory.  Few CTAs suffice to keep the link busy, so most SMs stay free
+// for the transform of the previous slab block.
+__global__ void __launch_bounds__(256) sym_gather_kernel(const double* __restrict__ hB, double* __restrict__ dB,
+                                                         int nb, int nbt, int64_t np) {
+    __shared__ double t[32][33];
+    const int64_t pairs = (int64_t)nbt * (nbt + 1) / 2;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    for (int64_t idx = blockIdx.x; idx < np * pairs; idx += gridDim.x) {
+        const int64_t P = idx / pairs;
+        int64_t q = idx % pairs;
+        int J = 0;
+        while (q >= J + 1) {  // column-block-major enumeration of (I, J), I <= J
+            q -= J + 1;
+            ++J;
+        }
+        const int I = (int)q;
+        const double* src = hB + P * (int64_t)nb * nb;
+        double* dst = dB + P * (int64_t)nb * nb;
+        // upper tile: rows mu = I*32 + tx, columns nu = J*32 + r
+        for (int r = ty; r < 32; r += 8) {
+            const int mu = I * 32 + tx, nu = J * 32 + r;
+            if (mu < nb && nu < nb && mu <= nu) {
+                const double v = src[mu + (int64_t)nb * nu];
+                t[r][tx] = v;
+                dst[mu + (int64_t)nb * nu] = v;
+            }
+        }
+        __syncthreads();
+        // mirror: rows nu = J*32 + tx, columns mu = I*32 + r, below the diagonal
+        for (int r = ty; r < 32; r += 8) {
+            const int nu = J * 32 + tx, mu = I * 32 + r;
+            if (mu < nb && nu < nb && nu > mu) dst[nu + (int64_t)nb * mu] = t[tx][r];
+        }
+        __syncthreads();
+    }
+}
+
+// Host-to-device copy of slabs P0 .. P0+np-1 of a symmetric ri3ao reading only
+// (about) the upper triangle: for each 32-column block J, rows 0 .. 32J+31 of
+// those columns of every slab form one 3-D box (row pitch nb, slab pitch nb^2).
+// Everything below the diagonal is then mirrored on the device.
+rt_status copy_symmetric_slabs(const double* hB, double* dB, int nb, int64_t np, cudaStream_t s) {
+    const int nbt = (nb + 31) / 32;
+    cudaPointerAttributes pa{};
+    if (cudaPointerGetAttributes(&pa, hB) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer) {
+        const double* dev_view = static_cast<const double*>(pa.devicePointer);
+        // Two CTAs per SM keep enough host reads in flight to fill the link (1, 0.5 and
+        // 0.1 per SM left it idle; 4 and 8 per SM took SMs from the transform).
+        sym_gather_kernel<<<2 * sm_count(), dim3(32, 8), 0, s>>>(dev_view, dB, nb, nbt, np);
+        return check_launch("sym_gather_kernel");
+    }
+    cudaGetLastError();  // pageable memory: no device view, take the copy path
+    for (int J = 0; J < nbt; ++J) {
+        const int c0 = 32 * J, c1 = std::min(nb, c0 + 32);
+        const int rows = std::min(nb, c0 + 32);
+        cudaMemcpy3DParms m = {};
+        m.srcPtr = make_cudaPitchedPtr(const_cast<double*>(hB) + (size_t)nb * c0, sizeof(double) * nb,
+                                       sizeof(double) * nb, nb);
+        m.dstPtr = make_cudaPitchedPtr(dB + (size_t)nb * c0, sizeof(double) * nb, sizeof(double) * nb, nb);
+        m.extent = make_cudaExtent(sizeof(double) * rows, (size_t)(c1 - c0), (size_t)np);
+        m.kind = cudaMemcpyHostToDevice;
+        RT_CUDA_TRY(cudaMemcpy3DAsync(&m, s));
+    }
+    const int64_t blocks = np * ((int64_t)nbt * (nbt + 1) / 2);
+    sym_mirror_kernel<<<(unsigned)blocks, dim3(32, 8), 0, s>>>(dB, nb, nbt, np);
+    return check_launch("sym_mirror_kernel");
+}
+
+// The pipelined host-pointer entry; symmetric: ri3ao slabs are symmetric and
+// only their upper triangles cross the host link.
+rt_status ri_ov_k_host_impl(const double* C, const double* B, int nb, int naux, int nocc, int nvir, double* ov,
+                            double* K, int form, int nslices, void* stream, bool symmetric) {
     RT_REQUIRE(nb >= 0 && naux >= 0 && nocc >= 0 && nvir >= 0, "rt_ri_ov_k_host: negative dimension");
     RT_REQUIRE(valid_form(form, nslices), "rt_ri_ov_k_host: bad form/nslices");
     cudaStream_t s = (cudaStream_t)stream;
@@ -444,7 +553,11 @@ rt_status rt_ri_ov_k_host(const double* C, const double* B, int nb, int naux, in
         st = RT_ERR_CUDA;
     };
     cudaError_t e;
-    if ((e = cudaStreamCreateWithFlags(&hs, cudaStreamNonBlocking)) != cudaSuccess) fail(e, "stream");
+    {
+        int lo = 0, hi = 0;  // the copy stream gets the highest priority: its CTAs go first
+        cudaDeviceGetStreamPriorityRange(&lo, &hi);
+        if ((e = cudaStreamCreateWithPriority(&hs, cudaStreamNonBlocking, hi)) != cudaSuccess) fail(e, "stream");
+    }
     if (st == RT_OK && (e = cudaStreamCreateWithFlags(&ds, cudaStreamNonBlocking)) != cudaSuccess) fail(e, "stream");
     if (st == RT_OK && (e = cudaEventCreateWithFlags(&ready, cudaEventDisableTiming)) != cudaSuccess) fail(e, "event");
     for (int64_t b = 0; st == RT_OK && b < nblk; ++b) {
@@ -473,8 +586,12 @@ rt_status rt_ri_ov_k_host(const double* C, const double* B, int nb, int naux, in
         };
         for (int64_t b = 0; st == RT_OK && b < nblk; ++b) {
             const int64_t P0 = b * blk, np = std::min<int64_t>(blk, naux - P0);
-            if ((e = cudaMemcpyAsync(dB.as<double>() + P0 * slab, B + P0 * slab, sizeof(double) * (size_t)(np * slab),
-                                     cudaMemcpyHostToDevice, hs)) != cudaSuccess) {
+            if (symmetric) {
+                st = copy_symmetric_slabs(B + P0 * slab, dB.as<double>() + P0 * slab, nb, np, hs);
+                if (st != RT_OK) break;
+            } else if ((e = cudaMemcpyAsync(dB.as<double>() + P0 * slab, B + P0 * slab,
+                                            sizeof(double) * (size_t)(np * slab), cudaMemcpyHostToDevice, hs)) !=
+                       cudaSuccess) {
                 fail(e, "host-to-device copy");
                 break;
             }
@@ -499,6 +616,23 @@ rt_status rt_ri_ov_k_host(const double* C, const double* B, int nb, int naux, in
     if (ds) cudaStreamDestroy(ds);
     if (st != RT_OK) return st;
     return error_word_check(s, "rt_ri_ov_k_host");
+}
+
+}  // namespace
+}  // namespace rt
+
+extern "C" {
+
+rt_status rt_ri_ov_k_host(const double* C, const double* B, int nb, int naux, int nocc, int nvir, double* ov,
+                          double* K, int form, int nslices, void* stream) {
+    NvtxRange nvtx_range("rt_ri_ov_k_host");
+    return ri_ov_k_host_impl(C, B, nb, naux, nocc, nvir, ov, K, form, nslices, stream, false);
+}
+
+rt_status rt_ri_ov_k_host_symmetric(const double* C, const double* B, int nb, int naux, int nocc, int nvir,
+                                    double* ov, double* K, int form, int nslices, void* stream) {
+    NvtxRange nvtx_range("rt_ri_ov_k_host_symmetric");
+    return ri_ov_k_host_impl(C, B, nb, naux, nocc, nvir, ov, K, form, nslices, stream, true);
 }
 
 // ------------------------------------------------------------ Fortran seam --

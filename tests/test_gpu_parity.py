@@ -283,3 +283,43 @@ def test_pipelined_host_entry_is_bitwise_equal_to_device_entry(form):
     rt.ri_ov_k_host(hC.data_ptr(), hB.data_ptr(), nb, naux, nocc, nvir, hO, hK, form=form, nslices=7)
     assert np.array_equal(hO, ov.cpu().numpy())
     assert np.array_equal(hK, K.cpu().numpy())
+
+
+@pytest.mark.parametrize("form", ["fp64", "split"])
+def test_symmetric_host_entry_is_bitwise_equal_to_device_entry(form):
+    # The synthetic ri3ao is exactly symmetric per slab, so reading only the
+    # upper triangles across the host link changes nothing.
+    nb, naux, nocc = 600, 300, 60
+    nvir = nb - nocc
+    B = rt.synth_ri3ao(11, nb, naux)
+    C = rt.synth_coef(11, nb)
+    ov, K = rt.ri_ov_k(C, B, nb, naux, nocc, nvir, form=form, nslices=7)
+    hB = torch.empty(B.numel(), dtype=torch.float64).pin_memory()
+    hB.copy_(B)
+    hO = np.zeros(nocc * nvir * naux)
+    hK = np.zeros(nb * nb)
+    rt.ri_ov_k_host(C.cpu().data_ptr(), hB.data_ptr(), nb, naux, nocc, nvir, hO, hK, form=form, nslices=7,
+                    symmetric=True)
+    assert np.array_equal(hO, ov.cpu().numpy())
+    assert np.array_equal(hK, K.cpu().numpy())
+
+
+@pytest.mark.parametrize("nb", [1, 31, 33, 100])
+def test_symmetric_host_entry_mirrors_the_upper_triangle(nb):
+    # Non-symmetric input: the result is that of the slabs symmetrised from their
+    # upper triangles (mu <= nu), for sizes around the 32-wide column blocks.
+    naux, nocc = 7, max(1, nb // 5)
+    nvir = nb - nocc
+    rng = np.random.default_rng(nb)
+    Bh = rng.standard_normal((nb, nb, naux))
+    up = np.triu(np.ones((nb, nb), dtype=bool))
+    Bsym = np.where(up[:, :, None], Bh, np.transpose(Bh, (1, 0, 2)))
+    C = oracle.synth_coef(nb, nb)
+    ov_ref, K_ref = oracle.ri_ov_k(C, Bsym, nocc)
+    hO = np.zeros(max(1, nocc * nvir * naux))
+    hK = np.zeros(nb * nb)
+    rt.ri_ov_k_host(np.asfortranarray(C), np.asfortranarray(Bh), nb, naux, nocc, nvir, hO, hK, form="fp64",
+                    symmetric=True)
+    if nvir:
+        assert relerr(hO[:nocc * nvir * naux].reshape(nocc, nvir, naux, order="F"), ov_ref) < 1e-12
+    assert relerr(hK.reshape(nb, nb, order="F"), K_ref) < 1e-12
