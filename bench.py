@@ -470,6 +470,25 @@ def main():
                 "slicing": {"kernel": "emax/slice kernels (HBM)", "achieved_gbs": s_bytes / s_ms / 1e6 if s_ms else None,
                             "peak_gbs": pk.get("hbm_gbs"), "share_of_step": s_ms / (ms * args.steps)}}
 
+    # ---- RI-J: two streaming passes over ri3ao (HBM-bound), timed on its own
+    w_j = torch.empty(NAUX, dtype=torch.float64, device=dev)
+    J_j = torch.empty(NB * NB, dtype=torch.float64, device=dev)
+    for _ in range(3):
+        rt.ri_j(B, D, NB, NAUX, w=w_j, J=J_j, stream=stream)
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(10):
+        rt.ri_j(B, D, NB, NAUX, w=w_j, J=J_j, stream=stream)
+    e1.record(stream)
+    barrier()
+    rij_ms = e0.elapsed_time(e1) / 10
+    rij_bytes = 2.0 * 8 * NB * NB * NAUX + 8.0 * 3 * NB * NB
+    rij = {"ms": rij_ms, "achieved_gbs": rij_bytes / rij_ms / 1e6, "peak_gbs": peaks()[0].get("hbm_gbs"),
+           "frac": rij_bytes / rij_ms / 1e6 / peaks()[0].get("hbm_gbs", FALLBACK_PEAKS["hbm_gbs"]),
+           "bytes": rij_bytes, "kernels": "rij_w_kernel + rij_j_kernel (float64, two reads of ri3ao)"}
+    del w_j, J_j
+
     # ---- end to end through the host-pointer C ABI (pinned host buffers)
     e2e = e2e_full = None
     if args.e2e_steps > 0:
@@ -536,7 +555,7 @@ def main():
                      "form": "float64 DFMA tiled GEMM"},
             "speedup_vs_fp64": fp64_ms / ms,
             "errors_vs_fp64": err, "gpu_launches": launches, "clocks": clocks, "roofline": roofline,
-            "e2e": e2e, "e2e_full_input": e2e_full, "cpu_baseline": cpu}
+            "e2e": e2e, "e2e_full_input": e2e_full, "rij": rij, "cpu_baseline": cpu}
     if sweep:
         line["sweep"] = sweep
     if batched:

@@ -396,18 +396,37 @@ namespace {
 __global__ void __launch_bounds__(256) rij_w_kernel(const double* __restrict__ B, const double* __restrict__ D,
                                                     int64_t n2, int naux, double* __restrict__ w) {
     __shared__ double red[8];
+    // 16-byte loads when every slab starts 16-byte aligned; four independent
+    // accumulators keep eight loads in flight per thread.
+    const bool vec = (n2 & 1) == 0 && ((uintptr_t)B & 15) == 0 && ((uintptr_t)D & 15) == 0;
     for (int P = blockIdx.x; P < naux; P += gridDim.x) {
         const double* b = B + (int64_t)P * n2;
-        double s0 = 0.0, s1 = 0.0;
-        int64_t e = threadIdx.x;
-        for (; e + 256 < n2; e += 512) {
-            s0 = fma(b[e], D[e], s0);
-            s1 = fma(b[e + 256], D[e + 256], s1);
+        double s[4] = {0.0, 0.0, 0.0, 0.0};
+        if (vec) {
+            const double2* b2 = reinterpret_cast<const double2*>(b);
+            const double2* d2 = reinterpret_cast<const double2*>(D);
+            const int64_t h = n2 / 2;
+            int64_t e = threadIdx.x;
+            for (; e + 768 < h; e += 1024) {
+                double2 x[4], y[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    x[u] = b2[e + 256 * u];
+                    y[u] = d2[e + 256 * u];
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) s[u] = fma(x[u].y, y[u].y, fma(x[u].x, y[u].x, s[u]));
+            }
+            for (; e < h; e += 256) {
+                const double2 x = b2[e], y = d2[e];
+                s[0] = fma(x.y, y.y, fma(x.x, y.x, s[0]));
+            }
+        } else {
+            for (int64_t e = threadIdx.x; e < n2; e += 256) s[0] = fma(b[e], D[e], s[0]);
         }
-        if (e < n2) s0 = fma(b[e], D[e], s0);
-        double s = s0 + s1;
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+        double t0 = (s[0] + s[1]) + (s[2] + s[3]);
+        for (int o = 16; o > 0; o >>= 1) t0 += __shfl_xor_sync(0xffffffffu, t0, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t0;
         __syncthreads();
         if (threadIdx.x < 32) {
             double t = threadIdx.x < 8 ? red[threadIdx.x] : 0.0;
@@ -434,6 +453,19 @@ __global__ void __launch_bounds__(256) rij_j_kernel(const double* __restrict__ B
             const double2* b2 = reinterpret_cast<const double2*>(B + e + (int64_t)P0 * n2);
             const int64_t st = n2 / 2;
             int p = 0;
+            // eight slabs in flight per thread
+            for (; p + 7 < np; p += 8) {
+                double2 x[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) x[u] = b2[(int64_t)(p + u) * st];
+#pragma unroll
+                for (int u = 0; u < 8; u += 2) {
+                    a0 = fma(ws[p + u], x[u].x, a0);
+                    a1 = fma(ws[p + u], x[u].y, a1);
+                    c0 = fma(ws[p + u + 1], x[u + 1].x, c0);
+                    c1 = fma(ws[p + u + 1], x[u + 1].y, c1);
+                }
+            }
             for (; p + 1 < np; p += 2) {
                 double2 x = b2[(int64_t)p * st], y = b2[(int64_t)(p + 1) * st];
                 a0 = fma(ws[p], x.x, a0);
