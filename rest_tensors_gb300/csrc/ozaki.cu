@@ -101,47 +101,17 @@ struct SliceArgs {
 
 template <int S>
 struct DigitConst {
-    // q has the row maximum's leading bit at position 61; digit s sits at bit
-    // 56 - 7 s, so the last digit's unit is 2^L.
+    // With t = R + off2, where R is the element in units of the last digit,
+    // digit k >= 1 is the 7-bit field at bit 7 (S-1-k), offset by 64; digit 0 is
+    // t >> 7 (S-1).  L is the last digit's bit position when the row maximum's
+    // leading bit sits at bit 61.
     static constexpr int L = 56 - 7 * (S - 1);
-    static constexpr unsigned long long off() {
+    static constexpr unsigned long long off2() {
         unsigned long long o = 0;
-        for (int k = 1; k < S; ++k) o += 1ull << (62 - 7 * k);
+        for (int k = 1; k < S; ++k) o += 64ull << (7 * (S - 1 - k));
         return o;
     }
 };
-
-// Signed base-128 digits of x relative to the row exponent emax (biased).
-// The last digit is rounded to nearest, ties to even; mantissa bits shifted
-// out below q are kept as a sticky bit, so only true ties go to even.  (Ties
-// are common when x is itself the output of this GEMM, whose results lie on a
-// coarse power-of-two grid; rounding ties away from zero would then bias |x|
-// upward.)
-template <int S>
-__device__ __forceinline__ void split_digits(double x, int emax, int (&d)[S]) {
-    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
-    const int e = (int)((bits >> 52) & 0x7FF);
-    const int sh = emax - e + 1;
-    if (e == 0 || sh >= 64) {
-#pragma unroll
-        for (int s = 0; s < S; ++s) d[s] = 0;
-        return;
-    }
-    const unsigned long long full = ((bits & 0xFFFFFFFFFFFFFull) | (1ull << 52)) << 10;
-    unsigned long long q = full >> sh;
-    q |= (full & ((1ull << sh) - 1ull)) != 0ull ? 1ull : 0ull;
-    constexpr int L = DigitConst<S>::L;
-    const unsigned long long t = q + ((1ull << (L - 1)) - 1ull) + ((q >> L) & 1ull) + DigitConst<S>::off();
-    const bool neg = (bits >> 63) != 0;
-    d[0] = (int)(t >> 56);
-#pragma unroll
-    for (int s = 1; s < S; ++s) d[s] = (int)((t >> (56 - 7 * s)) & 127ull) - 64;
-    if (neg) {
-#pragma unroll
-        for (int s = 0; s < S; ++s) d[s] = -d[s];
-    }
-}
-
 
 // -------------------------------------------------------------- row scale --
 
@@ -185,40 +155,47 @@ __global__ void emax_strided_kernel(Operand a, int64_t K, int64_t kspan, int* __
 
 // --------------------------------------------------------------- slicing --
 
-// Pack the S digit planes of 8 consecutive k of one row into 16-byte words.
-// The same digits as exact floats, at three operations per digit: a funnel
-// shift brings the 7-bit field (the digit + 64) to the low bits, one LOP3 masks
-// it and inserts the exponent of 2^23 (the float 2^23 + u), and one FMA by +-1
-// removes 2^23 + 64 and applies x's sign.  (split_digits states the digits
-// with integer arithmetic; both give the same values.)
+// Signed base-128 digits of x relative to the row exponent emax (biased), as
+// exact floats:  x ~= 2^(emax - 1028) * sum_s d_s 2^(-7 s),  |d_0| <= 65, |d_s| <= 64.
+// The element is rounded once, to nearest with ties to even, at the last
+// digit's unit: with m the 53-bit mantissa, that unit is bit P = emax - e + L - 9
+// of m, so R = RNE(m / 2^P).  (Ties are common when x is itself the output of
+// this GEMM, whose results lie on a coarse power-of-two grid; rounding ties
+// away from zero would bias |x| upward.)  Each digit then costs three
+// operations: a funnel shift brings its 7-bit field (digit + 64) to the low
+// bits, one LOP3 masks it and inserts the exponent of 2^23 (the float 2^23 + u),
+// and one FMA by +-1 removes 2^23 + 64 and applies x's sign.
 template <int S>
 __device__ __forceinline__ void split_digits_f(double x, int emax, float (&f)[S]) {
     const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
     const int e = (int)((bits >> 52) & 0x7FF);
-    const int sh = emax - e + 1;
-    if (e == 0 || sh >= 64) {
+    constexpr int L = DigitConst<S>::L;
+    const int P = emax - e + L - 9;
+    if (e == 0 || P >= 54) {  // zero, subnormal, or below half a unit of the last digit
 #pragma unroll
         for (int s = 0; s < S; ++s) f[s] = 0.0f;
         return;
     }
-    const unsigned long long full = ((bits & 0xFFFFFFFFFFFFFull) | (1ull << 52)) << 10;
-    unsigned long long q = full >> sh;
-    q |= (full & ((1ull << sh) - 1ull)) != 0ull ? 1ull : 0ull;
-    constexpr int L = DigitConst<S>::L;
-    const unsigned long long t = q + ((1ull << (L - 1)) - 1ull) + ((q >> L) & 1ull) + DigitConst<S>::off();
+    const unsigned long long m = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    unsigned long long R;
+    if (L - 9 <= 0 && P <= 0) R = m << (-P);  // S = 8 only: the grid is finer than the mantissa
+    else R = (m + ((1ull << (P - 1)) - 1ull) + ((m >> P) & 1ull)) >> P;
+    const unsigned long long t = R + DigitConst<S>::off2();
     const uint32_t hi = (uint32_t)(t >> 32), lo = (uint32_t)t;
     const float sg = (bits >> 63) ? -1.0f : 1.0f;
-    // leading digit: t >> 56, no bias
-    f[0] = __fmaf_rn(__uint_as_float((hi >> 24) | 0x4B000000u), sg, -8388608.0f * sg);
+    constexpr int p0 = 7 * (S - 1);
+    const uint32_t w0 = p0 >= 32 ? (hi >> (p0 - 32)) : __funnelshift_r(lo, hi, p0);
+    f[0] = __fmaf_rn(__uint_as_float(w0 | 0x4B000000u), sg, -8388608.0f * sg);
     const float c = -8388672.0f * sg;  // -(2^23 + 64) * sign
 #pragma unroll
     for (int s = 1; s < S; ++s) {
-        const int pos = 56 - 7 * s;
+        const int pos = 7 * (S - 1 - s);
         const uint32_t win = pos >= 32 ? (hi >> (pos - 32)) : __funnelshift_r(lo, hi, pos);
         f[s] = __fmaf_rn(__uint_as_float((win & 127u) | 0x4B000000u), sg, c);
     }
 }
 
+// Pack the S digit planes of 8 consecutive k of one row into 16-byte words.
 template <int S>
 __device__ __forceinline__ void digits8(const double (&x)[8], int em, uint32_t (&w)[S][4]) {
 #pragma unroll

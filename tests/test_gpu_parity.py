@@ -296,9 +296,10 @@ def test_symmetric_host_entry_is_bitwise_equal_to_device_entry(form):
     ov, K = rt.ri_ov_k(C, B, nb, naux, nocc, nvir, form=form, nslices=7)
     hB = torch.empty(B.numel(), dtype=torch.float64).pin_memory()
     hB.copy_(B)
+    hC = C.cpu()  # held for the call: the entry reads it through a raw address
     hO = np.zeros(nocc * nvir * naux)
     hK = np.zeros(nb * nb)
-    rt.ri_ov_k_host(C.cpu().data_ptr(), hB.data_ptr(), nb, naux, nocc, nvir, hO, hK, form=form, nslices=7,
+    rt.ri_ov_k_host(hC.data_ptr(), hB.data_ptr(), nb, naux, nocc, nvir, hO, hK, form=form, nslices=7,
                     symmetric=True)
     assert np.array_equal(hO, ov.cpu().numpy())
     assert np.array_equal(hK, K.cpu().numpy())
