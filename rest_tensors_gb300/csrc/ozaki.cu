@@ -144,11 +144,10 @@ __global__ void emax_strided_kernel(Operand a, int64_t K, int64_t kspan, int* __
     if (r >= a.rows) return;
     const int64_t k0 = (int64_t)blockIdx.y * kspan, k1 = min(K, k0 + kspan);
     const double* base = a.p + (r % a.div) * a.s0 + (r / a.div) * a.s1;
-    unsigned int m = 0;
-    for (int64_t k = k0; k < k1; ++k) {
-        const unsigned int e = ((unsigned int)__double2hiint(base[k * a.sk]) >> 20) & 0x7FFu;
-        m = max(m, e);
-    }
+    unsigned int m = 0;  // maximum of the sign-cleared high words
+    const double* src = base + k0 * a.sk;
+    for (int64_t k = k0; k < k1; ++k, src += a.sk) m = max(m, (unsigned int)__double2hiint(*src) & 0x7FFFFFFFu);
+    m >>= 20;
     if (m == 0x7FFu) atomicOr(err, DEV_ERR_NONFINITE);
     if (m) atomicMax(&emax[r], (int)m);
 }
@@ -235,10 +234,14 @@ __global__ void __launch_bounds__(256) slice_strided_kernel(SliceArgs a) {
         const int em = valid ? a.emax[row] : 0;
         const double* base = valid ? a.src.p + (row % a.src.div) * a.src.s0 + (row / a.src.div) * a.src.s1 : nullptr;
         double x[8];
+        const int64_t k0 = k32 * SK + q * 8;
+        const double* src = base + k0 * a.src.sk;
+        if (valid && k0 + 8 <= a.K) {
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const int64_t k = k32 * SK + q * 8 + j;
-            x[j] = (valid && k < a.K) ? base[k * a.src.sk] : 0.0;
+            for (int j = 0; j < 8; ++j) x[j] = src[j * a.src.sk];
+        } else {
+#pragma unroll
+            for (int j = 0; j < 8; ++j) x[j] = (valid && k0 + j < a.K) ? src[j * a.src.sk] : 0.0;
         }
         uint32_t w[S][4];
         digits8<S>(x, em, w);
@@ -266,17 +269,24 @@ __global__ void __launch_bounds__(256, RR >= 16 ? 2 : 3)
     const bool valid = row < a.src.rows;
     const double* base = valid ? a.src.p + (row % a.src.div) * a.src.s0 + (row / a.src.div) * a.src.s1 : nullptr;
     double x[NBLK][8];
+    // Maximum of the sign-cleared high words: its exponent field is the row's.
     unsigned int m = 0;
+    const int64_t sk = a.src.sk;
 #pragma unroll
     for (int j = 0; j < NBLK; ++j) {
         const int64_t k0 = (int64_t)(kq + KQN * j) * 8;
+        const double* src = base + k0 * sk;
+        if (valid && k0 + 8 <= a.K) {  // whole run inside k: no per-element tests
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            const int64_t k = k0 + i;
-            x[j][i] = (valid && k < a.K) ? base[k * a.src.sk] : 0.0;
-            m = max(m, ((unsigned int)__double2hiint(x[j][i]) >> 20) & 0x7FFu);
+            for (int i = 0; i < 8; ++i) x[j][i] = src[i * sk];
+        } else {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) x[j][i] = (valid && k0 + i < a.K) ? src[i * sk] : 0.0;
         }
+#pragma unroll
+        for (int i = 0; i < 8; ++i) m = max(m, (unsigned int)__double2hiint(x[j][i]) & 0x7FFFFFFFu);
     }
+    m >>= 20;
     // lanes r, r + RR, ... of a warp share the row; then across the 8 warps
 #pragma unroll
     for (int o = RR; o < 32; o <<= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
@@ -316,17 +326,21 @@ __global__ void __launch_bounds__(256, 2) slice_contig_rowmax_kernel(SliceArgs a
     const bool valid = row < a.src.rows;
     const double* base = valid ? a.src.p + (row % a.src.div) * a.src.s0 + (row / a.src.div) * a.src.s1 : nullptr;
     double x[NBLK][8];
-    unsigned int m = 0;
+    unsigned int m = 0;  // maximum of the sign-cleared high words
 #pragma unroll
     for (int j = 0; j < NBLK; ++j) {
         const int64_t k0 = (int64_t)(kq + 16 * j) * 8;
+        if (valid && k0 + 8 <= a.K) {
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            const int64_t k = k0 + i;
-            x[j][i] = (valid && k < a.K) ? base[k] : 0.0;
-            m = max(m, ((unsigned int)__double2hiint(x[j][i]) >> 20) & 0x7FFu);
+            for (int i = 0; i < 8; ++i) x[j][i] = base[k0 + i];
+        } else {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) x[j][i] = (valid && k0 + i < a.K) ? base[k0 + i] : 0.0;
         }
+#pragma unroll
+        for (int i = 0; i < 8; ++i) m = max(m, (unsigned int)__double2hiint(x[j][i]) & 0x7FFFFFFFu);
     }
+    m >>= 20;
     // lanes r, r+8, r+16, r+24 share the row within a warp; then 4 warps
     m = max(m, __shfl_xor_sync(0xffffffffu, m, 8));
     m = max(m, __shfl_xor_sync(0xffffffffu, m, 16));
