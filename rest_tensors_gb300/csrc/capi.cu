@@ -72,6 +72,9 @@ rt_status ri_ao2mo_split(const double* C, const double* B, double* R, int nb, in
 
 // Half-transform and ov block for slabs [P0, P0 + np) of B (B already offset to slab P0):
 //   X^P = B^P C_occ  ->  X[mu + nb i + nb nocc P],   ov[i,a,P] = (X^P^T C_vir)[i,a].
+// chunks_per_item for "the whole contraction range in one work item".
+constexpr int kWholeRange = 1 << 30;
+
 rt_status ri_ov_block(const double* C, const double* B, int nb, int64_t np, int nocc, int nvir, double* X,
                       double* ov, int form, int S, cudaStream_t stream) {
     const int64_t per = (int64_t)nb * nocc;
@@ -100,6 +103,10 @@ rt_status ri_ov_block(const double* C, const double* B, int nb, int64_t np, int 
     g1.B.p = C; g1.B.rows = nocc; g1.B.s0 = nb; g1.B.sk = 1;
     g1.C.p = X; g1.C.md = nb; g1.C.ms0 = 1; g1.C.ms1 = per; g1.C.ns0 = nb;
     g1.nslices = S;
+    // No split-K for the two transform products: a CTA's int64 range guard
+    // depends on the terms it sums, so results then do not depend on how the
+    // slabs are blocked (the host entry streams them in blocks of any size).
+    g1.chunks_per_item = kWholeRange;
     RT_TRY(oz_gemm(g1, stream));
     if (ov && nvir > 0) {
         // A(m=(i,P), k=mu) = X[mu + nb m], B(n=a, k=mu) = C_vir[mu + nb a]
@@ -109,6 +116,7 @@ rt_status ri_ov_block(const double* C, const double* B, int nb, int64_t np, int 
         g2.B.p = C + per; g2.B.rows = nvir; g2.B.s0 = nb; g2.B.sk = 1;
         g2.C.p = ov; g2.C.md = nocc; g2.C.ms0 = 1; g2.C.ms1 = (int64_t)nocc * nvir; g2.C.ns0 = nocc;
         g2.nslices = S;
+        g2.chunks_per_item = kWholeRange;
         RT_TRY(oz_gemm(g2, stream));
     }
     return RT_OK;
@@ -543,7 +551,16 @@ rt_status ri_ov_k_host_impl(const double* C, const double* B, int nb, int naux, 
     // Slab blocks of ~512 MB: host-to-device copies of block b+1 run on their own
     // stream while block b is transformed; ov blocks go back on a third stream.
     const int64_t blk = std::max<int64_t>(1, std::min<int64_t>(naux, ((int64_t)64 << 20) / std::max<int64_t>(slab, 1)));
-    const int64_t nblk = ceil_div(naux, blk);
+    // Block boundaries: full blocks, then a short last block (a sixth of one), so
+    // that little transform work is left once the last slabs have arrived.
+    std::vector<int64_t> bstart;
+    {
+        const int64_t tail = naux > blk ? std::max<int64_t>(1, blk / 6) : naux;
+        for (int64_t P = 0; P < naux - tail; P += blk) bstart.push_back(P);
+        bstart.push_back(naux - tail);
+        bstart.push_back(naux);
+    }
+    const int64_t nblk = (int64_t)bstart.size() - 1;
     cudaStream_t hs = nullptr, ds = nullptr;
     cudaEvent_t ready = nullptr;
     std::vector<cudaEvent_t> in(nblk, nullptr), out(nblk, nullptr);
@@ -571,7 +588,7 @@ rt_status ri_ov_k_host_impl(const double* C, const double* B, int nb, int naux, 
         cudaStreamWaitEvent(hs, ready, 0);
         cudaStreamWaitEvent(ds, ready, 0);
         auto compute = [&](int64_t b) -> rt_status {
-            const int64_t P0 = b * blk, np = std::min<int64_t>(blk, naux - P0);
+            const int64_t P0 = bstart[b], np = bstart[b + 1] - bstart[b];
             cudaStreamWaitEvent(s, in[b], 0);
             RT_TRY(ri_ov_block(dC.as<double>(), dB.as<double>() + P0 * slab, nb, np, nocc, nvir,
                                dX.as<double>() + P0 * per, (ov && nO) ? dO.as<double>() + P0 * oslab : nullptr, form,
@@ -585,7 +602,7 @@ rt_status ri_ov_k_host_impl(const double* C, const double* B, int nb, int naux, 
             return RT_OK;
         };
         for (int64_t b = 0; st == RT_OK && b < nblk; ++b) {
-            const int64_t P0 = b * blk, np = std::min<int64_t>(blk, naux - P0);
+            const int64_t P0 = bstart[b], np = bstart[b + 1] - bstart[b];
             if (symmetric) {
                 st = copy_symmetric_slabs(B + P0 * slab, dB.as<double>() + P0 * slab, nb, np, hs);
                 if (st != RT_OK) break;
