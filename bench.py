@@ -61,6 +61,8 @@ def parse():
     p.add_argument("--batch-mols", type=int, default=64, help="molecules of the batched uneven-size leg (0: skip)")
     p.add_argument("--batch-steps", type=int, default=20)
     p.add_argument("--large", type=int, default=1, help="run the nbas=1200 / naux=4800 system with Davidson (0: skip)")
+    p.add_argument("--outputs", type=int, default=1,
+                   help="also time the full ri3mo transform and the (ia|jb) block of this workload (0: skip)")
     p.add_argument("--large-steps", type=int, default=3)
     return p.parse_args()
 
@@ -281,6 +283,49 @@ def large_leg(args, rt, torch, stream):
     del B, ov, K
     torch.cuda.empty_cache()
     return out
+
+
+# -------------------------------------------------- other outputs of config 2 --
+def outputs_leg(args, rt, torch, stream, B, C, ov):
+    """The full ri3mo transform [naux, nbas, nbas] and the (ia|jb) block (nocc nvir)^2,
+    split form against the float64 form (one timed call each after a warm-up)."""
+    S = args.nslices
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        rt.sync_status()
+        return out, e0.elapsed_time(e1)
+
+    res = {}
+    # ri3mo: naux (2 nb^2 ns + 2 nb ns^2) with ns = nb
+    fl = NAUX * 4.0 * NB ** 3
+    r64 = torch.empty(NAUX * NB * NB, dtype=torch.float64, device="cuda")
+    rsp = torch.empty_like(r64)
+    _, ms64 = timed(lambda: rt.ri_ao2mo(C, B, NB, NB, NAUX, out=r64, form="fp64", stream=stream))
+    _, mssp = timed(lambda: rt.ri_ao2mo(C, B, NB, NB, NAUX, out=rsp, form="split", nslices=S, stream=stream))
+    res["ri3mo"] = {"shape": [NAUX, NB, NB], "flop": fl, "split": {"ms": mssp, "tflops": fl / mssp / 1e9},
+                    "fp64": {"ms": ms64, "tflops": fl / ms64 / 1e9}, "speedup_vs_fp64": ms64 / mssp,
+                    "max_abs_err": float((rsp - r64).abs().max())}
+    del r64, rsp
+    # (ia|jb) = sum_P B_ia^P B_jb^P, B_ov = ov as [nocc nvir, naux]
+    nov = NOCC * NVIR
+    fl = 2.0 * nov * nov * NAUX
+    m64 = torch.empty(nov * nov, dtype=torch.float64, device="cuda")
+    msp = torch.empty_like(m64)
+    _, ms64 = timed(lambda: rt.ri_iajb(ov, nov, NAUX, M=m64, form="fp64", stream=stream))
+    _, mssp = timed(lambda: rt.ri_iajb(ov, nov, NAUX, M=msp, form="split", nslices=S, stream=stream))
+    res["iajb"] = {"shape": [nov, nov], "flop": fl, "split": {"ms": mssp, "tflops": fl / mssp / 1e9},
+                   "fp64": {"ms": ms64, "tflops": fl / ms64 / 1e9}, "speedup_vs_fp64": ms64 / mssp,
+                   "max_rel_err": float((msp - m64).abs().max() / m64.abs().max())}
+    del m64, msp
+    torch.cuda.empty_cache()
+    return res
 
 
 # ------------------------------------------------------------ CPU baseline --
@@ -526,6 +571,10 @@ def main():
                     "path": "rt_ri_ov_k_host (C ABI, pinned host buffers, whole ri3ao copied)"}
         del hB
 
+    outputs = None
+    if args.outputs:
+        outputs = outputs_leg(args, rt, torch, stream, B, C, ov)
+
     batched = None
     if args.batch_mols > 0:
         del ov, K
@@ -558,6 +607,8 @@ def main():
             "e2e": e2e, "e2e_full_input": e2e_full, "rij": rij, "cpu_baseline": cpu}
     if sweep:
         line["sweep"] = sweep
+    if outputs:
+        line["outputs"] = outputs
     if batched:
         line["batched"] = batched
     if large:
