@@ -64,6 +64,8 @@ def parse():
     p.add_argument("--outputs", type=int, default=1,
                    help="also time the full ri3mo transform and the (ia|jb) block of this workload (0: skip)")
     p.add_argument("--large-steps", type=int, default=3)
+    p.add_argument("--ri3fn", type=int, default=1,
+                   help="also time the ri3fn metric step (special_dgemm_f_01) on this workload's tensor (0: skip)")
     return p.parse_args()
 
 
@@ -328,6 +330,116 @@ def outputs_leg(args, rt, torch, stream, B, C, ov):
     return res
 
 
+# ------------------------------------------------ ri3fn metric step (special_dgemm_f_01) --
+def ri3fn_leg(args, rt, torch, stream, B):
+    """The O_V V^{-1/2} step of the ri3fn preparation on this workload's tensor
+    [nbas, nbas, naux]: every (mu, nu) row times an [naux, naux] matrix, in place.
+    The matrix is an orthogonal stand-in for V^{-1/2} (Q of a seeded QR).
+    Split and float64 forms are timed once each after a warm-up; both are checked
+    on three nu-slices against the oracle's float64 product on the host, and an
+    OpenBLAS sample on the host cores gives the CPU rate."""
+    import numpy as np
+
+    S = args.nslices
+    M = rt.synth_coef(args.seed + 7, NAUX)
+    size_a, size_b = (NB, NB, NAUX), (NAUX, NAUX)
+    fl = 2.0 * NB * NB * NAUX * NAUX
+
+    def call(T, form):
+        rt.special_dgemm_01(T, size_a, range(NB), range(NAUX), M, size_b, range(NAUX), range(NAUX), 1.0, 0.0,
+                            form=form, nslices=S, stream=stream)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        rt.sync_status()
+        return e0.elapsed_time(e1)
+
+    T = B.clone()
+    call(T, "split")  # warm-up (scratch pool, kernels)
+    T.copy_(B)
+    ms_sp = timed(lambda: call(T, "split"))
+    T64 = B.clone()
+    ms_64 = timed(lambda: call(T64, "fp64"))
+    Mh = M.cpu().numpy().reshape(NAUX, NAUX, order="F")
+    Bv = B.view(NAUX, NB, NB)  # [P][nu][mu]
+    errs = {"split": 0.0, "fp64": 0.0}
+    for nu in (0, NB // 2 + 1, NB - 1):
+        slab = Bv[:, nu, :].cpu().numpy().T  # [mu, P]
+        want = slab @ Mh
+        scale = float(np.abs(want).max())
+        for name, t in (("split", T), ("fp64", T64)):
+            got = t.view(NAUX, NB, NB)[:, nu, :].cpu().numpy().T
+            errs[name] = max(errs[name], float(np.abs(got - want).max()) / scale)
+    split_vs_fp64 = float((T - T64).abs().max() / T64.abs().max())
+    del T, T64
+    torch.cuda.empty_cache()
+    res = {"shape": {"ten3_a": list(size_a), "matr_b": list(size_b)}, "flop": fl,
+           "split": {"ms": ms_sp, "tflops": fl / ms_sp / 1e9},
+           "fp64": {"ms": ms_64, "tflops": fl / ms_64 / 1e9}, "speedup_vs_fp64": ms_64 / ms_sp,
+           "max_rel_err_vs_oracle": errs, "split_vs_fp64_max_rel": split_vs_fp64,
+           "matr_b": "orthogonal stand-in for V^-1/2 (Q of a seeded N(0,1) QR)"}
+    if not args.no_cpu:
+        import oracle
+
+        oracle.set_threads(os.cpu_count() or 1)
+        ny = 32
+        rng = np.random.default_rng(args.seed)
+        t = rng.standard_normal(NB * ny * NAUX)
+        oracle.special_dgemm_f_01(t, (NB, ny, NAUX), (0, NB), (0, NAUX), Mh.reshape(-1, order="F"), size_b,
+                                  (0, NAUX), (0, NAUX), 1.0, 0.0)  # warm-up
+        t0 = time.perf_counter()
+        oracle.special_dgemm_f_01(t, (NB, ny, NAUX), (0, NB), (0, NAUX), Mh.reshape(-1, order="F"), size_b,
+                                  (0, NAUX), (0, NAUX), 1.0, 0.0)
+        dt = time.perf_counter() - t0
+        res["cpu"] = {"tflops": 2.0 * NB * ny * NAUX * NAUX / dt / 1e12, "cores": oracle.get_threads(),
+                      "sample": f"{ny} of {NB} nu-slices, C restatement of restmatr.f90:111-154 over OpenBLAS",
+                      "seconds": dt}
+    return res
+
+
+# ------------------------------------------------------------- layout utilities --
+def layout_leg(args, rt, torch, stream, B):
+    """RIFull transposes and the symmetric pair packing on this workload's ri3ao
+    tensor [nbas, nbas, naux] (6.9 GB): bytes moved per call (read + write) over
+    CUDA-event time, as GB/s and as a fraction of the measured copy rate."""
+    hbm = peaks()[0]["hbm_gbs"]
+    nel = NB * NB * NAUX
+    out = torch.empty(nel, dtype=torch.float64, device="cuda")
+    res = {}
+
+    def timed(fn, reps=5):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        rt.sync_status()
+        return e0.elapsed_time(e1) / reps
+
+    for order in ("jik", "jki", "kji", "ikj"):
+        ms = timed(lambda: rt.ri_transpose(B, (NB, NB, NAUX), order, out=out, stream=stream))
+        gbs = 16.0 * nel / ms / 1e6
+        res["transpose_" + order] = {"ms": ms, "gbs": gbs, "frac_of_copy": gbs / hbm}
+    npair = NB * (NB + 1) // 2
+    ms = timed(lambda: rt.ri_pack_symm(B, NB, NAUX, out=out, stream=stream))
+    gbs = 16.0 * npair * NAUX / ms / 1e6
+    res["pack_symm"] = {"ms": ms, "gbs": gbs, "frac_of_copy": gbs / hbm}
+    res["note"] = ("inputs 6.9 GB (larger than L2); transposes count one read of the input and one write of the "
+                   "output; pack_symm counts the upper triangles it reads and writes (3.46 GB each); copy rate "
+                   "from the measured peaks")
+    del out
+    torch.cuda.empty_cache()
+    return res
+
+
 # ------------------------------------------------------------ CPU baseline --
 def cpu_baseline(seed: int, budget_s: float = 12.0):
     """Oracle (C restatement of restmatr.f90 + OpenBLAS, all host threads) on a bounded slab range."""
@@ -575,6 +687,11 @@ def main():
     if args.outputs:
         outputs = outputs_leg(args, rt, torch, stream, B, C, ov)
 
+    ri3fn = None
+    if args.ri3fn:
+        ri3fn = ri3fn_leg(args, rt, torch, stream, B)
+        ri3fn["layout"] = layout_leg(args, rt, torch, stream, B)
+
     batched = None
     if args.batch_mols > 0:
         del ov, K
@@ -609,6 +726,8 @@ def main():
         line["sweep"] = sweep
     if outputs:
         line["outputs"] = outputs
+    if ri3fn:
+        line["ri3fn"] = ri3fn
     if batched:
         line["batched"] = batched
     if large:

@@ -88,6 +88,24 @@ void general_dgemm_f_(const double* matr_a, const int* rows_a, const int* column
                       const int* len_row_c, const int* start_column_c, const int* len_column_c,
                       const double* alpha, const double* beta);
 
+/* Replaces special_dgemm_f_01_ (src/external_libs/ffi_restmatr.rs:25-33,
+ * restmatr.f90:111-154; Rust wrapper src/external_libs/mod.rs:85-99), the
+ * O_V * V^{-1/2} step of the ri3fn preparation.  For every y-slice of the
+ * column-major host tensor ten3_a[x_a, y_a, z_a]:
+ *   T = ten3_a[sx:sx+lx, y, sz:sz+lz]
+ *   T <- alpha * T * matr_b[rb:rb+lz, cb:cb+lz] + beta * T
+ * with 0-based starts and lengths.  The block of matr_b must be lz x lz.
+ * i_y_a is accepted and ignored, as in the Fortran, which loops over all
+ * y-slices.  The Fortran body hands one buffer to dgemm as both A and C; this
+ * entry computes the product those arguments describe, from an unaliased
+ * copy.  Float64 form.  Failures are reported through rt_last_status() /
+ * rt_last_error() and leave ten3_a unchanged. */
+void special_dgemm_f_01_(double* ten3_a, const int* x_a, const int* y_a, const int* z_a, const int* start_x_a,
+                         const int* len_x_a, const int* i_y_a, const int* start_z_a, const int* len_z_a,
+                         const double* matr_b, const int* rows_b, const int* columns_b, const int* start_row_b,
+                         const int* len_row_b, const int* start_column_b, const int* len_column_b,
+                         const double* alpha, const double* beta);
+
 /* ------------------------------------------------------------------------
  * Device-pointer API.
  * ------------------------------------------------------------------------ */
@@ -106,6 +124,16 @@ rt_status rt_dgemm(char opa, char opb, int m, int n, int k, double alpha, const 
  * update: one set of digit planes, one triangle, mirrored. */
 rt_status rt_dgemm_split(char opa, char opb, int m, int n, int k, const double* A, int lda, const double* B, int ldb,
                          double* C, int ldc, int nslices, void* stream);
+
+/* special_dgemm_f_01_ on device memory and a stream: the same operation on
+ * ten3_a[x_a, y_a, z_a] and matr_b[rows_b, columns_b], in place.  form
+ * RT_FORM_FP64, or RT_FORM_SPLIT (nslices 3..8), whose product runs on the
+ * tensor cores and then applies alpha and beta in float64.  Scratch: at most
+ * 8 GB of staged y-slices (plus the split form's digit planes). */
+rt_status rt_special_dgemm_01(double* ten3_a, int x_a, int y_a, int z_a, int start_x_a, int len_x_a, int start_z_a,
+                              int len_z_a, const double* matr_b, int rows_b, int columns_b, int start_row_b,
+                              int len_row_b, int start_column_b, int len_column_b, double alpha, double beta,
+                              int form, int nslices, void* stream);
 
 /* Full AO->MO transform, RIFull::ao2mo (src/ri.rs:356-408):
  *   ri3mo[P,p,q] = (C^T B^P C)[p,q],  C = [nb, ns], B = [nb, nb, naux] symmetric in (mu, nu).
@@ -171,6 +199,49 @@ rt_status rt_ri_j(const double* B, const double* D, int nb, int naux, double* w,
 /* Exchange energy E_x = -tr(D K) = -sum_{mu,nu} D[mu,nu] K[mu,nu], reduced in
  * float64 with a fixed-order tree.  Writes one double to ex_device. */
 rt_status rt_ri_exchange_energy(const double* D, const double* K, int nb, double* ex_device, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Layout utilities (device pointers).  Blocks are given by 0-based starts
+ * and lengths; a source and target that share memory behave as a Fortran
+ * array assignment (the source is read in full before the target is written).
+ * ------------------------------------------------------------------------ */
+
+/* copy_mm (restmatr.f90:197-212; Rust matr_copy, src/external_libs/mod.rs:102-120):
+ *   t_matr[tx:tx+x_len, ty:ty+y_len] = f_matr[fx:fx+x_len, fy:fy+y_len] */
+rt_status rt_copy_mm(int x_len, int y_len, const double* f_matr, int f_x_len, int f_y_len, int f_x_start,
+                     int f_y_start, double* t_matr, int t_x_len, int t_y_len, int t_x_start, int t_y_start,
+                     void* stream);
+
+/* copy_mr (restmatr.f90:215-238; Rust ri_copy_from_matr, mod.rs:145-165): a
+ * matrix block [x1_len, x2_len] into the rank-3 tensor t_ri[X, Y, Z] at
+ *   mode 0: t_ri[a, b, t_x3]   mode 1: t_ri[a, t_x3, b]   mode 2: t_ri[t_x3, a, b]
+ * with a = t_x1_start.., b = t_x2_start...  Other modes: RT_ERR_INVALID_ARG
+ * (the Fortran silently copies nothing). */
+rt_status rt_copy_mr(int x1_len, int x2_len, const double* f_matr, int f_x_len, int f_y_len, int f_x1_start,
+                     int f_x2_start, double* t_ri, int t_x_len, int t_y_len, int t_z_len, int t_x1_start,
+                     int t_x2_start, int t_x3, int mode, void* stream);
+
+/* copy_rm (restmatr.f90:237-264; Rust matr_copy_from_ri, mod.rs:123-140): the
+ * reverse of copy_mr, from f_ri[X, Y, Z] (same modes) into a matrix block. */
+rt_status rt_copy_rm(int x1_len, int x2_len, const double* f_ri, int f_x_len, int f_y_len, int f_z_len,
+                     int f_x1_start, int f_x2_start, int f_x3, int mode, double* t_matr, int t_x_len, int t_y_len,
+                     int t_x1_start, int t_x2_start, void* stream);
+
+/* copy_rr (restmatr.f90:266-285; Rust ri_copy_from_ri, mod.rs:168-190): a
+ * [x1_len, x2_len, x3_len] block between two rank-3 tensors. */
+rt_status rt_copy_rr(int x1_len, int x2_len, int x3_len, const double* f_ri, int f_x1_len, int f_x2_len,
+                     int f_x3_len, int f_x1_start, int f_x2_start, int f_x3_start, double* t_ri, int t_x1_len,
+                     int t_x2_len, int t_x3_len, int t_x1_start, int t_x2_start, int t_x3_start, void* stream);
+
+/* RIFull transposes (src/ri.rs:225-295): `in` is [i, j, k]; `order` names the
+ * output's axes, e.g. "jik" -> [j, i, k] (transpose_jik), "jki", "kji", "ikj"
+ * (any permutation of "ijk" is accepted):  out[.. in the named order ..] = in[a_i, a_j, a_k]. */
+rt_status rt_ri_transpose(const double* in, int i, int j, int k, const char* order, double* out, void* stream);
+
+/* rifull_to_matfull_symm (src/ri.rs:296-307, 330-341): [nao, nao, naux] ->
+ * [nao (nao + 1) / 2, naux], keeping rows r <= column c of every slab, packed
+ * column after column: out[c (c + 1) / 2 + r, P] = in[r, c, P]. */
+rt_status rt_ri_pack_symm(const double* in, int nao, int naux, double* out, void* stream);
 
 /* ------------------------------------------------------------------------
  * Response operator and Davidson solver.
@@ -269,9 +340,13 @@ rt_status rt_profile_get(int kind, double* total_ms, long long* launches, double
  * that nothing arrives at, for at most `cycles` clock cycles (<= 2e9), then sets
  * the device error word's timeout flag and returns normally; rt_sync_status()
  * then reports RT_ERR_TIMEOUT.  This is the library's bounded-wait path run out
- * on purpose; no device fault is raised. */
+ * on purpose; no device fault is raised.
+ * rt_debug_chunk_bytes(bytes): bound on the scratch of one staged chunk of
+ * y-slices in rt_special_dgemm_01 (default 8 GB; bytes <= 0 restores it), so
+ * that small tensors can run through several chunks.  Process-wide. */
 rt_status rt_debug_fail_alloc_after(long long n);
 rt_status rt_debug_wait_timeout(long long cycles, void* stream);
+rt_status rt_debug_chunk_bytes(long long bytes);
 
 #ifdef __cplusplus
 }

@@ -192,6 +192,126 @@ def full_to_upper_packed(m) -> np.ndarray:
 
 
 # --------------------------------------------------------------------------
+# ri3fn preparation and layout utilities
+# --------------------------------------------------------------------------
+def special_dgemm_f_01(ten3, size_a, range_x_a, range_z_a, matr_b, size_b, range_row_b, range_column_b,
+                       alpha, beta):
+    """restmatr.f90:111-154 (through oracle.c) on flat column-major data; ranges are (start, stop).
+
+    Returns the updated tensor as a new flat array; ``ten3`` is not modified.
+    """
+    t = np.array(np.asarray(ten3, dtype=np.float64).reshape(-1), copy=True)
+    b = np.ascontiguousarray(np.asarray(matr_b, dtype=np.float64).reshape(-1))
+    i = ctypes.c_int
+    lib().oracle_special_dgemm_f_01(
+        _p(t), i(size_a[0]), i(size_a[1]), i(size_a[2]), i(range_x_a[0]), i(range_x_a[1] - range_x_a[0]),
+        i(range_z_a[0]), i(range_z_a[1] - range_z_a[0]), _p(b), i(size_b[0]), i(size_b[1]), i(range_row_b[0]),
+        i(range_row_b[1] - range_row_b[0]), i(range_column_b[0]), i(range_column_b[1] - range_column_b[0]),
+        ctypes.c_double(alpha), ctypes.c_double(beta))
+    return t
+
+
+def _fview(flat, size):
+    return np.asarray(flat).reshape(tuple(size), order="F")
+
+
+def copy_mm(x_len, y_len, f, f_size, f_start, t, t_size, t_start):
+    """restmatr.f90:197-212: t[tx:tx+x_len, ty:ty+y_len] = f[fx:fx+x_len, fy:fy+y_len] (flat arrays; t updated)."""
+    F, T = _fview(f, f_size), _fview(t, t_size)
+    T[t_start[0]:t_start[0] + x_len, t_start[1]:t_start[1] + y_len] = \
+        F[f_start[0]:f_start[0] + x_len, f_start[1]:f_start[1] + y_len].copy()
+    return t
+
+
+def _ri_block(R, a0, alen, b0, blen, fix, mode):
+    if mode == 0:
+        return (slice(a0, a0 + alen), slice(b0, b0 + blen), fix)
+    if mode == 1:
+        return (slice(a0, a0 + alen), fix, slice(b0, b0 + blen))
+    if mode == 2:
+        return (fix, slice(a0, a0 + alen), slice(b0, b0 + blen))
+    return None
+
+
+def copy_mr(x1_len, x2_len, f, f_size, f_start, t, t_size, t_start, t_x3, mode):
+    """restmatr.f90:215-238: a matrix block into rank-3 t by mode 0/1/2 (other modes copy nothing)."""
+    F, T = _fview(f, f_size), _fview(t, t_size)
+    idx = _ri_block(T, t_start[0], x1_len, t_start[1], x2_len, t_x3, mode)
+    if idx is not None:
+        T[idx] = F[f_start[0]:f_start[0] + x1_len, f_start[1]:f_start[1] + x2_len].copy()
+    return t
+
+
+def copy_rm(x1_len, x2_len, f, f_size, f_start, f_x3, mode, t, t_size, t_start):
+    """restmatr.f90:241-264: the reverse of copy_mr."""
+    F, T = _fview(f, f_size), _fview(t, t_size)
+    idx = _ri_block(F, f_start[0], x1_len, f_start[1], x2_len, f_x3, mode)
+    if idx is not None:
+        T[t_start[0]:t_start[0] + x1_len, t_start[1]:t_start[1] + x2_len] = F[idx].copy()
+    return t
+
+
+def copy_rr(lens, f, f_size, f_start, t, t_size, t_start):
+    """restmatr.f90:266-285: a [x1, x2, x3] block between rank-3 tensors."""
+    F, T = _fview(f, f_size), _fview(t, t_size)
+    T[tuple(slice(t_start[d], t_start[d] + lens[d]) for d in range(3))] = \
+        F[tuple(slice(f_start[d], f_start[d] + lens[d]) for d in range(3))].copy()
+    return t
+
+
+# The RIFull transposes restated with the reference's own enumeration
+# (src/ri.rs:226-294), in pure Python: small tensors only.
+def transpose_jik(data, size):
+    """ri.rs:226-238: each [i, j] chunk of the slab order is transposed."""
+    i, j, k = size
+    out = []
+    for z in range(k):
+        chunk = data[z * i * j:(z + 1) * i * j]
+        out.extend(chunk[r + c * i] for r in range(i) for c in range(j))
+    return out
+
+
+def transpose_jki(data, size):
+    """ri.rs:240-256: for each ii, the elements whose flat index is congruent to ii mod i, in order."""
+    i, j, k = size
+    out = []
+    for ii in range(i):
+        out.extend(v for idx, v in enumerate(data) if abs(idx - ii) % i == 0)
+    return out
+
+
+def transpose_kji(data, size):
+    """ri.rs:258-275: transpose_jik, then for each ij the elements congruent to ij mod i*j."""
+    i, j, k = size
+    t = transpose_jik(data, size)
+    out = []
+    for ij in range(i * j):
+        out.extend(v for idx, v in enumerate(t) if abs(idx - ij) % (i * j) == 0)
+    return out
+
+
+def transpose_ikj(data, size):
+    """ri.rs:277-294: for each jj, column jj of every [i, j] slab."""
+    i, j, k = size
+    out = []
+    for jj in range(j):
+        for z in range(k):
+            chunk = data[z * i * j:(z + 1) * i * j]
+            out.extend(chunk[jj * i:(jj + 1) * i])
+    return out
+
+
+def rifull_to_matfull_symm(data, nao, naux):
+    """ri.rs:296-307 with richunk_reduce_by_symm (ri.rs:330-341): rows 0..=c of column c, per slab."""
+    out = []
+    for P in range(naux):
+        chunk = data[P * nao * nao:(P + 1) * nao * nao]
+        for c in range(nao):
+            out.extend(chunk[c * nao:c * nao + c + 1])
+    return out
+
+
+# --------------------------------------------------------------------------
 # Synthetic inputs
 # --------------------------------------------------------------------------
 def synth_ri3ao(seed, nb, naux, P0=0, P1=None):

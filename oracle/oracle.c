@@ -256,6 +256,45 @@ int oracle_dsyev(char jobz, int n, double* a, double* w) {
     return info;
 }
 
+/*
+ * restmatr.f90:111-154 special_dgemm_f_01 (the O_V * V^{-1/2} step of the
+ * ri3fn preparation).  For i_state = 1..y_a (i_y_a is never read) the Fortran
+ * copies the section T = ten3_a(sx+1:sx+lx, i_state, sz+1:sz+lz) into
+ * matr_c, calls
+ *   dgemm('N','N', lx, len_column_b, lz, alpha, matr_c, lx,
+ *         matr_b(section), lz, beta, matr_c, lx)
+ * and copies matr_c back into the same section.  matr_b's section reaches
+ * dgemm as a gfortran copy-in temporary with leading dimension lz.  The
+ * Fortran passes matr_c as both A and C, which BLAS does not define; this
+ * restatement gives dgemm a separate copy of T as A, which is the product
+ * the arguments describe.
+ */
+void oracle_special_dgemm_f_01(double* ten3_a, int x_a, int y_a, int z_a, int start_x_a, int len_x_a,
+                               int start_z_a, int len_z_a, const double* matr_b, int rows_b, int columns_b,
+                               int start_row_b, int len_row_b, int start_column_b, int len_column_b,
+                               double alpha, double beta) {
+    (void)z_a; (void)columns_b;
+    const int lx = len_x_a, lz = len_z_a, n = len_column_b;
+    if (lx <= 0 || lz <= 0 || n <= 0) return;
+    const size_t xy = (size_t)x_a * (size_t)y_a;
+    double* ta = (double*)malloc(sizeof(double) * (size_t)lx * (size_t)lz);
+    double* tc = (double*)malloc(sizeof(double) * (size_t)lx * (size_t)n);
+    double* tb = (double*)malloc(sizeof(double) * (size_t)len_row_b * (size_t)len_column_b);
+    copy_block_in(matr_b, rows_b, start_row_b, len_row_b, start_column_b, len_column_b, tb);
+    for (int i = 0; i < y_a; ++i) {
+        for (int z = 0; z < lz; ++z)
+            memcpy(ta + (size_t)z * lx, ten3_a + (size_t)start_x_a + (size_t)i * x_a + (size_t)(start_z_a + z) * xy,
+                   sizeof(double) * (size_t)lx);
+        for (int z = 0; z < n; ++z) memcpy(tc + (size_t)z * lx, ta + (size_t)z * lx, sizeof(double) * (size_t)lx);
+        int m = lx, k = lz, ld = lx, ldb = lz;
+        p_dgemm("N", "N", &m, &n, &k, &alpha, ta, &ld, tb, &ldb, &beta, tc, &ld);
+        for (int z = 0; z < n; ++z)
+            memcpy(ten3_a + (size_t)start_x_a + (size_t)i * x_a + (size_t)(start_z_a + z) * xy, tc + (size_t)z * lx,
+                   sizeof(double) * (size_t)lx);
+    }
+    free(ta); free(tb); free(tc);
+}
+
 /* ------------------------------------------------------------------------ */
 /* Synthetic inputs (same formulas as the device generator)                  */
 /* ------------------------------------------------------------------------ */

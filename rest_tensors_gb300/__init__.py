@@ -130,6 +130,23 @@ def lib() -> ctypes.CDLL:
     L.rt_debug_fail_alloc_after.argtypes = [ctypes.c_longlong]
     L.rt_debug_wait_timeout.restype = c_int
     L.rt_debug_wait_timeout.argtypes = [ctypes.c_longlong, vp]
+    L.rt_debug_chunk_bytes.restype = c_int
+    L.rt_debug_chunk_bytes.argtypes = [ctypes.c_longlong]
+    L.rt_special_dgemm_01.restype = c_int
+    L.rt_special_dgemm_01.argtypes = [vp] + [c_int] * 7 + [vp] + [c_int] * 6 + [c_dbl, c_dbl, c_int, c_int, vp]
+    L.rt_copy_mm.restype = c_int
+    L.rt_copy_mm.argtypes = [c_int, c_int, vp, c_int, c_int, c_int, c_int, vp, c_int, c_int, c_int, c_int, vp]
+    L.rt_copy_mr.restype = c_int
+    L.rt_copy_mr.argtypes = [c_int, c_int, vp, c_int, c_int, c_int, c_int, vp] + [c_int] * 7 + [vp]
+    L.rt_copy_rm.restype = c_int
+    L.rt_copy_rm.argtypes = [c_int, c_int, vp] + [c_int] * 7 + [vp, c_int, c_int, c_int, c_int, vp]
+    L.rt_copy_rr.restype = c_int
+    L.rt_copy_rr.argtypes = [c_int] * 3 + [vp] + [c_int] * 6 + [vp] + [c_int] * 6 + [vp]
+    L.rt_ri_transpose.restype = c_int
+    L.rt_ri_transpose.argtypes = [vp, c_int, c_int, c_int, ctypes.c_char_p, vp, vp]
+    L.rt_ri_pack_symm.restype = c_int
+    L.rt_ri_pack_symm.argtypes = [vp, c_int, c_int, vp, vp]
+    L.special_dgemm_f_01_.restype = None
     L.ri_ao2mo_f_.restype = None
     L.general_dgemm_f_.restype = None
     _lib = L
@@ -246,6 +263,22 @@ def general_dgemm_f(matr_a: np.ndarray, size_a, range_row_a, range_column_a, opa
                        _hp(matr_b), r(i(size_b[0])), r(i(size_b[1])), rb, lb, cb, lcb, r(ctypes.c_char(opb.encode())),
                        _hp(matr_c), r(i(size_c[0])), r(i(size_c[1])), rc, lc, cc, lcc,
                        r(ctypes.c_double(alpha)), r(ctypes.c_double(beta)))
+    _check(last_status())
+
+
+def special_dgemm_f_01(ten3_a: np.ndarray, size_a, range_x_a: range, i_y: int, range_z_a: range,
+                       matr_b: np.ndarray, size_b, range_row_b: range, range_column_b: range, alpha: float,
+                       beta: float) -> None:
+    """src/external_libs/mod.rs:85-99 -> special_dgemm_f_01_: in place on the host tensor ten3_a[size_a],
+    every y-slice block times matr_b[range_row_b, range_column_b] (see restmatr.f90:111-154)."""
+    L = lib()
+    i = ctypes.c_int
+    r = ctypes.byref
+    L.special_dgemm_f_01_(_hp(ten3_a), r(i(size_a[0])), r(i(size_a[1])), r(i(size_a[2])), r(i(range_x_a.start)),
+                          r(i(len(range_x_a))), r(i(i_y)), r(i(range_z_a.start)), r(i(len(range_z_a))),
+                          _hp(matr_b), r(i(size_b[0])), r(i(size_b[1])), r(i(range_row_b.start)),
+                          r(i(len(range_row_b))), r(i(range_column_b.start)), r(i(len(range_column_b))),
+                          r(ctypes.c_double(alpha)), r(ctypes.c_double(beta)))
     _check(last_status())
 
 
@@ -374,6 +407,65 @@ def ri_ov_k_host(C: np.ndarray, B: np.ndarray, nb: int, naux: int, nocc: int, nv
 
     fn = lib().rt_ri_ov_k_host_symmetric if symmetric else lib().rt_ri_ov_k_host
     _check(fn(hp(C), hp(B), nb, naux, nocc, nvir, hp(ov), hp(K), _form(form), nslices, _stream(stream)))
+
+
+def special_dgemm_01(ten3, size_a, range_x_a: range, range_z_a: range, matr_b, size_b, range_row_b: range,
+                     range_column_b: range, alpha: float = 1.0, beta: float = 0.0, form: str = "fp64",
+                     nslices: int = DEFAULT_NSLICES, stream=None) -> None:
+    """special_dgemm_f_01 on device tensors (flat, column-major), in place on ``ten3``."""
+    _check(lib().rt_special_dgemm_01(
+        _dptr(ten3), size_a[0], size_a[1], size_a[2], range_x_a.start, len(range_x_a), range_z_a.start,
+        len(range_z_a), _dptr(matr_b), size_b[0], size_b[1], range_row_b.start, len(range_row_b),
+        range_column_b.start, len(range_column_b), alpha, beta, _form(form), nslices, _stream(stream)))
+
+
+def copy_mm(x_len: int, y_len: int, f_matr, f_size, f_start, t_matr, t_size, t_start, stream=None) -> None:
+    """restmatr.f90:197-212 on device matrices: t[ts.., ..] = f[fs.., ..] for an x_len x y_len block."""
+    _check(lib().rt_copy_mm(x_len, y_len, _dptr(f_matr), f_size[0], f_size[1], f_start[0], f_start[1],
+                            _dptr(t_matr), t_size[0], t_size[1], t_start[0], t_start[1], _stream(stream)))
+
+
+def copy_mr(x1_len: int, x2_len: int, f_matr, f_size, f_start, t_ri, t_size, t_start, t_x3: int, mode: int,
+            stream=None) -> None:
+    """restmatr.f90:215-238 on device data: a matrix block into a rank-3 tensor (mode 0, 1 or 2)."""
+    _check(lib().rt_copy_mr(x1_len, x2_len, _dptr(f_matr), f_size[0], f_size[1], f_start[0], f_start[1],
+                            _dptr(t_ri), t_size[0], t_size[1], t_size[2], t_start[0], t_start[1], t_x3, mode,
+                            _stream(stream)))
+
+
+def copy_rm(x1_len: int, x2_len: int, f_ri, f_size, f_start, f_x3: int, mode: int, t_matr, t_size, t_start,
+            stream=None) -> None:
+    """restmatr.f90:241-264 on device data: a rank-3 tensor block into a matrix (mode 0, 1 or 2)."""
+    _check(lib().rt_copy_rm(x1_len, x2_len, _dptr(f_ri), f_size[0], f_size[1], f_size[2], f_start[0], f_start[1],
+                            f_x3, mode, _dptr(t_matr), t_size[0], t_size[1], t_start[0], t_start[1],
+                            _stream(stream)))
+
+
+def copy_rr(lens, f_ri, f_size, f_start, t_ri, t_size, t_start, stream=None) -> None:
+    """restmatr.f90:266-285 on device data: a block between rank-3 tensors."""
+    _check(lib().rt_copy_rr(lens[0], lens[1], lens[2], _dptr(f_ri), f_size[0], f_size[1], f_size[2], f_start[0],
+                            f_start[1], f_start[2], _dptr(t_ri), t_size[0], t_size[1], t_size[2], t_start[0],
+                            t_start[1], t_start[2], _stream(stream)))
+
+
+def ri_transpose(ri, size, order: str, out=None, stream=None):
+    """RIFull transpose_<order> (src/ri.rs:226-294) of a device [i, j, k] tensor, e.g. order="jki"."""
+    import torch
+
+    if out is None:
+        out = torch.empty(int(size[0]) * int(size[1]) * int(size[2]), dtype=torch.float64, device=ri.device)
+    _check(lib().rt_ri_transpose(_dptr(ri), size[0], size[1], size[2], order.encode(), _dptr(out), _stream(stream)))
+    return out
+
+
+def ri_pack_symm(ri, nao: int, naux: int, out=None, stream=None):
+    """rifull_to_matfull_symm (src/ri.rs:296-307): [nao, nao, naux] -> [nao (nao + 1) / 2, naux]."""
+    import torch
+
+    if out is None:
+        out = torch.empty(max(nao * (nao + 1) // 2 * naux, 1), dtype=torch.float64, device=ri.device)
+    _check(lib().rt_ri_pack_symm(_dptr(ri), nao, naux, _dptr(out), _stream(stream)))
+    return out[: nao * (nao + 1) // 2 * naux]
 
 
 def ri_j(B, D, nb: int, naux: int, w=None, J=None, stream=None):
@@ -548,6 +640,11 @@ def davidson_ri_response(Bov, delta, nov: int, naux: int, x0_1d, params: Davidso
 def debug_fail_alloc_after(n: int) -> None:
     """Testing hook: the next n scratch allocations succeed, the one after fails (n < 0: off)."""
     _check(lib().rt_debug_fail_alloc_after(n))
+
+
+def debug_chunk_bytes(nbytes: int) -> None:
+    """Testing hook: scratch bound of one staged chunk in special_dgemm_01 (<= 0 restores 8 GB)."""
+    _check(lib().rt_debug_chunk_bytes(int(nbytes)))
 
 
 def debug_wait_timeout(cycles: int, stream=None) -> None:

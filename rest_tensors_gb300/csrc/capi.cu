@@ -1,23 +1,15 @@
 // capi.cu - the exported C ABI: the reference's Fortran seam (drop-in, host
 // pointers) and the rt_* device-pointer API, composed from the float64 and
 // split-precision GEMM services.
-#include <nvtx3/nvToolsExt.h>
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <vector>
 
 #include "rt_internal.cuh"
 
 namespace rt {
-
-// NVTX range over one entry point (visible in Nsight timelines; no cost without a tool).
-struct NvtxRange {
-    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
-    ~NvtxRange() { nvtxRangePop(); }
-    NvtxRange(const NvtxRange&) = delete;
-    NvtxRange& operator=(const NvtxRange&) = delete;
-};
 
 
 rt_status ri_j_fp64(const double* B, const double* D, int nb, int naux, double* w, double* J, cudaStream_t stream);
@@ -162,6 +154,86 @@ rt_status ri_ov_k_split(const double* C, const double* B, int nb, int naux, int 
     return RT_OK;
 }
 
+// Scratch bound of one staged chunk of the ri3fn metric contraction
+// (rt_debug_chunk_bytes lowers it for tests).
+constexpr int64_t kMetricChunkBytes = (int64_t)8 << 30;
+std::atomic<long long> g_chunk_bytes{kMetricChunkBytes};
+
+// blk(xx, i, z) = alpha * blk(xx, i, z) + beta * S(xx, i, z) over the block
+// [lx, ny, lz]; blk at xx + X i + XY z, S contiguous.
+__global__ void __launch_bounds__(256) scale_add_block_kernel(double* __restrict__ blk,
+                                                              const double* __restrict__ S, int64_t lx, int64_t ny,
+                                                              int64_t lz, int64_t X, int64_t XY, double alpha,
+                                                              double beta) {
+    const int64_t nrow = ny * lz;
+    for (int64_t r = blockIdx.y; r < nrow; r += gridDim.y) {
+        const int64_t i = r % ny, z = r / ny;
+        double* d = blk + i * X + z * XY;
+        const double* src = S + r * lx;
+        for (int64_t xx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; xx < lx;
+             xx += (int64_t)gridDim.x * blockDim.x) {
+            const double v = beta == 0.0 ? 0.0 : beta * src[xx];
+            d[xx] = fma(alpha, d[xx], v);
+        }
+    }
+}
+
+// special_dgemm_f_01 (restmatr.f90:111-154) on device memory: for every
+// y-slice of the rank-3 tensor T[X, Y, Z],
+//   T[sx:sx+lx, y, sz:sz+lz] <- alpha * T[...] * M[srb:srb+lz, scb:scb+lz] + beta * T[...]
+// Chunks of y-slices are staged in scratch (the product reads its left
+// operand there), then written back in place: by the float64 GEMM with alpha
+// and beta applied in its epilogue, or by the split GEMM followed by one
+// scale-add pass when (alpha, beta) != (1, 0).
+rt_status special_dgemm_01(double* T, int64_t X, int64_t Y, int64_t sx, int64_t lx, int64_t sz, int64_t lz,
+                           const double* Mb, int64_t rows_b, int64_t srb, int64_t scb, double alpha, double beta,
+                           int form, int S, cudaStream_t stream) {
+    const int64_t XY = X * Y;
+    const int64_t per_y = lx * lz;
+    const int64_t chunk = g_chunk_bytes.load(std::memory_order_relaxed);
+    const int64_t yc = std::max<int64_t>(1, std::min<int64_t>(Y, chunk / (8 * per_y)));
+    ScratchBuf sb;
+    RT_TRY(scratch_alloc(sb, sizeof(double) * (size_t)(per_y * yc), stream));
+    double* St = sb.as<double>();
+    const double* Msub = Mb + srb + rows_b * scb;
+    for (int64_t y0 = 0; y0 < Y; y0 += yc) {
+        const int64_t ny = std::min<int64_t>(yc, Y - y0);
+        const int64_t M = lx * ny;
+        double* blk = T + sx + X * y0 + XY * sz;
+        Copy3 c;
+        c.n[0] = lx; c.n[1] = ny; c.n[2] = lz;
+        c.is[0] = 1; c.is[1] = X; c.is[2] = XY;
+        c.os[0] = 1; c.os[1] = lx; c.os[2] = M;
+        RT_TRY(strided_copy3(blk, St, c, stream));
+        if (form == RT_FORM_FP64) {
+            GemmF64 g;
+            g.opa = 'N'; g.opb = 'N';
+            g.m = M; g.n = lz; g.k = lz; g.alpha = alpha; g.beta = beta;
+            g.A = St; g.lda = M;
+            g.B = Msub; g.ldb = rows_b;
+            g.C = blk; g.rsC = 1; g.csC = XY; g.c_md = lx; g.c_ms1 = X;
+            RT_TRY(gemm_f64(g, stream));
+        } else {
+            // C(m, n) = sum_k A(m, k) B(n, k): A = the staged rows, B(n, k) = Msub(k, n).
+            OzGemm g;
+            g.K = lz;
+            g.A.p = St; g.A.rows = M; g.A.s0 = 1; g.A.sk = M;
+            g.B.p = Msub; g.B.rows = lz; g.B.s0 = rows_b; g.B.sk = 1;
+            g.C.p = blk; g.C.md = lx; g.C.ms0 = 1; g.C.ms1 = X; g.C.ns0 = XY;
+            g.nslices = S;
+            RT_TRY(oz_gemm(g, stream));
+            if (alpha != 1.0 || beta != 0.0) {
+                const int64_t nrow = ny * lz;
+                const unsigned gx = (unsigned)std::min<int64_t>((lx + 255) / 256, 8);
+                const unsigned gy = (unsigned)std::min<int64_t>(nrow, 65535);
+                scale_add_block_kernel<<<dim3(gx, gy), 256, 0, stream>>>(blk, St, lx, ny, lz, X, XY, alpha, beta);
+                RT_TRY(check_launch("scale_add_block_kernel"));
+            }
+        }
+    }
+    return RT_OK;
+}
+
 bool valid_form(int form, int nslices) {
     return form == RT_FORM_FP64 || (form == RT_FORM_SPLIT && nslices >= 3 && nslices <= 8);
 }
@@ -224,6 +296,34 @@ rt_status rt_dgemm_split(char opa, char opb, int m, int n, int k, const double* 
         g.symmetric = true;
     }
     return oz_gemm(g, s);
+}
+
+rt_status rt_debug_chunk_bytes(long long bytes) {
+    g_chunk_bytes.store(bytes <= 0 ? kMetricChunkBytes : bytes);
+    return RT_OK;
+}
+
+rt_status rt_special_dgemm_01(double* ten3_a, int x_a, int y_a, int z_a, int start_x_a, int len_x_a, int start_z_a,
+                              int len_z_a, const double* matr_b, int rows_b, int columns_b, int start_row_b,
+                              int len_row_b, int start_column_b, int len_column_b, double alpha, double beta,
+                              int form, int nslices, void* stream) {
+    NvtxRange nvtx_range("rt_special_dgemm_01");
+    RT_REQUIRE(x_a >= 0 && y_a >= 0 && z_a >= 0 && rows_b >= 0 && columns_b >= 0,
+               "rt_special_dgemm_01: negative dimension");
+    RT_REQUIRE(valid_form(form, nslices), "rt_special_dgemm_01: bad form/nslices (%d, %d)", form, nslices);
+    RT_REQUIRE(start_x_a >= 0 && len_x_a >= 0 && (int64_t)start_x_a + len_x_a <= x_a && start_z_a >= 0 &&
+                   len_z_a >= 0 && (int64_t)start_z_a + len_z_a <= z_a,
+               "rt_special_dgemm_01: block of ten3_a outside the tensor");
+    RT_REQUIRE(start_row_b >= 0 && len_row_b >= 0 && (int64_t)start_row_b + len_row_b <= rows_b &&
+                   start_column_b >= 0 && len_column_b >= 0 && (int64_t)start_column_b + len_column_b <= columns_b,
+               "rt_special_dgemm_01: block of matr_b outside the matrix");
+    RT_REQUIRE(len_row_b == len_z_a && len_column_b == len_z_a,
+               "rt_special_dgemm_01: the block of matr_b must be len_z_a x len_z_a (got %d x %d, len_z_a %d)",
+               len_row_b, len_column_b, len_z_a);
+    if ((int64_t)len_x_a * y_a * len_z_a == 0) return RT_OK;
+    RT_REQUIRE(ten3_a && matr_b, "rt_special_dgemm_01: null pointer");
+    return special_dgemm_01(ten3_a, x_a, y_a, start_x_a, len_x_a, start_z_a, len_z_a, matr_b, rows_b, start_row_b,
+                            start_column_b, alpha, beta, form, nslices, (cudaStream_t)stream);
 }
 
 rt_status rt_ri_ao2mo(const double* C, const double* B, double* ri3mo, int nb, int ns, int naux, int form,
@@ -738,6 +838,58 @@ void general_dgemm_f_(const double* matr_a, const int* rows_a, const int* column
         return RT_OK;
     };
     if (run() != RT_OK) fprintf(stderr, "general_dgemm_f_: %s\n", rt_last_error());
+}
+
+void special_dgemm_f_01_(double* ten3_a, const int* x_a, const int* y_a, const int* z_a, const int* start_x_a,
+                         const int* len_x_a, const int* i_y_a, const int* start_z_a, const int* len_z_a,
+                         const double* matr_b, const int* rows_b, const int* columns_b, const int* start_row_b,
+                         const int* len_row_b, const int* start_column_b, const int* len_column_b,
+                         const double* alpha, const double* beta) {
+    NvtxRange nvtx_range("special_dgemm_f_01_");
+    rt::set_error(RT_OK, "");
+    (void)i_y_a;  // the Fortran loops over every y-slice and never reads it
+    auto run = [&]() -> rt_status {
+        const int X = *x_a, Y = *y_a, Z = *z_a, lx = *len_x_a, lz = *len_z_a;
+        RT_REQUIRE(X >= 0 && Y >= 0 && Z >= 0, "special_dgemm_f_01_: negative dimension");
+        RT_REQUIRE(*start_x_a >= 0 && lx >= 0 && (int64_t)*start_x_a + lx <= X && *start_z_a >= 0 && lz >= 0 &&
+                       (int64_t)*start_z_a + lz <= Z,
+                   "special_dgemm_f_01_: block of ten3_a outside the tensor");
+        RT_REQUIRE(*start_row_b >= 0 && *len_row_b >= 0 && (int64_t)*start_row_b + *len_row_b <= *rows_b &&
+                       *start_column_b >= 0 && *len_column_b >= 0 &&
+                       (int64_t)*start_column_b + *len_column_b <= *columns_b,
+                   "special_dgemm_f_01_: block of matr_b outside the matrix");
+        RT_REQUIRE(*len_row_b == lz && *len_column_b == lz,
+                   "special_dgemm_f_01_: the block of matr_b must be len_z_a x len_z_a");
+        if ((int64_t)lx * Y * lz == 0) return RT_OK;
+        cudaStream_t s = cudaStreamPerThread;
+        const size_t blk_elems = (size_t)lx * Y * lz;
+        ScratchBuf dT, dM;
+        RT_TRY(scratch_alloc(dT, sizeof(double) * blk_elems, s));
+        RT_TRY(scratch_alloc(dM, sizeof(double) * (size_t)lz * lz, s));
+        // The block [lx, Y, lz] as a contiguous device tensor.
+        cudaMemcpy3DParms up = {};
+        up.srcPtr = make_cudaPitchedPtr(ten3_a, sizeof(double) * X, sizeof(double) * X, Y);
+        up.srcPos = make_cudaPos(sizeof(double) * *start_x_a, 0, *start_z_a);
+        up.dstPtr = make_cudaPitchedPtr(dT.p, sizeof(double) * lx, sizeof(double) * lx, Y);
+        up.extent = make_cudaExtent(sizeof(double) * lx, Y, lz);
+        up.kind = cudaMemcpyHostToDevice;
+        RT_CUDA_TRY(cudaMemcpy3DAsync(&up, s));
+        RT_CUDA_TRY(cudaMemcpy2DAsync(dM.p, sizeof(double) * lz,
+                                      matr_b + (size_t)*start_column_b * *rows_b + *start_row_b,
+                                      sizeof(double) * *rows_b, sizeof(double) * lz, lz, cudaMemcpyHostToDevice, s));
+        RT_TRY(special_dgemm_01(dT.as<double>(), lx, Y, 0, lx, 0, lz, dM.as<double>(), lz, 0, 0, *alpha, *beta,
+                                RT_FORM_FP64, 0, s));
+        cudaMemcpy3DParms down = {};
+        down.srcPtr = up.dstPtr;
+        down.dstPtr = up.srcPtr;
+        down.dstPos = up.srcPos;
+        down.extent = up.extent;
+        down.kind = cudaMemcpyDeviceToHost;
+        RT_CUDA_TRY(cudaMemcpy3DAsync(&down, s));
+        RT_CUDA_TRY(cudaStreamSynchronize(s));
+        return RT_OK;
+    };
+    if (run() != RT_OK) fprintf(stderr, "special_dgemm_f_01_: %s\n", rt_last_error());
 }
 
 }  // extern "C"

@@ -6,6 +6,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 #include <stdio.h>
 
@@ -83,11 +84,27 @@ enum : unsigned int {
 
 int sm_count();
 
+// NVTX range over one entry point (visible in Nsight timelines; no cost without a tool).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
+
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
 // "No composite index": a divisor larger than any row count.
 constexpr int64_t kNoDiv = (int64_t)1 << 62;
+
+// Strided block copy of float64 elements, the primitive under the layout
+// utilities:  out[a0 os0 + a1 os1 + a2 os2] = in[a0 is0 + a1 is1 + a2 is2]
+// for a_d < n[d].  Source and destination must not overlap.
+struct Copy3 {
+    int64_t n[3] = {1, 1, 1}, is[3] = {0, 0, 0}, os[3] = {0, 0, 0};
+};
+rt_status strided_copy3(const double* in, double* out, const Copy3& c, cudaStream_t stream);
 
 // FP64 GEMM service used by every plain-form contraction.  Column-major.
 //   C_b(i,j) = alpha * sum_k opA(A_b)(i,k) opB(B_b)(k,j) + beta * C_b(i,j)
