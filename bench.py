@@ -402,6 +402,64 @@ def ri3fn_leg(args, rt, torch, stream, B):
     return res
 
 
+# --------------------------------------------------- Newton-Schulz inverse square root --
+def newton_schulz_leg(args, rt, torch, stream):
+    """_newton_schulz_inverse_square_root_v02 on a [naux, naux] symmetric positive stand-in for the
+    Coulomb metric V: Q diag(d) Q^T with d uniform in [0.5, 3] (seeded) and Q the seeded orthogonal
+    matrix of the ri3fn leg.  The reference's own parameters: threshold 1e-8 scaled to 1e-10, mixing
+    1.0, 100 iterations, level shift [0.0].  Both forms once after a warm-up, and the oracle on the
+    host cores."""
+    import numpy as np
+
+    n = NAUX
+    Q = rt.synth_coef(args.seed + 7, n).view(n, n)  # column-major: Q[col][row]
+    d = torch.from_numpy(np.random.default_rng(args.seed + 11).uniform(0.5, 3.0, n)).cuda()
+    S = (Q.t() * d) @ Q  # [row][col] view of a symmetric matrix; its flat data is the column-major matrix
+    S = (0.5 * (S + S.t())).contiguous().view(-1)
+    args_ns = (1e-10, 1.0, 100, [0.0])
+
+    def run(form):
+        return rt.newton_schulz_inverse_square_root_v02(S, n, *args_ns, form=form, nslices=args.nslices,
+                                                         stream=stream)
+
+    res = {"n": n, "threshold": 1e-10, "mix_parameter": 1.0, "num_iter": 100, "level_shift": [0.0],
+           "matrix": "Q diag(d) Q^T, d ~ U[0.5, 3], stand-in for the Coulomb metric"}
+    outs = {}
+    for form in ("split", "fp64"):
+        run(form)  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        X, _, conv, evals = run(form)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        fl = evals * 3 * 2.0 * n ** 3
+        res[form] = {"ms": dt * 1e3, "converged": conv, "evaluations": evals, "tflops": fl / dt / 1e12}
+        outs[form] = X
+    Xf = outs["fp64"].view(n, n)
+    Sm = S.view(n, n)
+    res["fp64"]["max_abs_residual_XSX_minus_I"] = float((Xf @ Sm @ Xf - torch.eye(n, dtype=torch.float64,
+                                                                                 device="cuda")).abs().max())
+    res["split_vs_fp64_max_rel"] = float((outs["split"] - outs["fp64"]).abs().max() / outs["fp64"].abs().max())
+    res["speedup_vs_fp64"] = res["fp64"]["ms"] / res["split"]["ms"]
+    res["timing"] = "host clock around the call (it synchronises once per evaluation)"
+    if not args.no_cpu:
+        import oracle
+
+        oracle.set_threads(os.cpu_count() or 1)
+        Sh = S.cpu().numpy().reshape(n, n, order="F")
+        t0 = time.perf_counter()
+        Xo, _, conv_o, evals_o = oracle.newton_schulz_inverse_square_root_v02(Sh, *args_ns)
+        dt = time.perf_counter() - t0
+        res["cpu"] = {"ms": dt * 1e3, "converged": conv_o, "evaluations": evals_o,
+                      "tflops": evals_o * 6.0 * n ** 3 / dt / 1e12, "cores": oracle.get_threads(),
+                      "sample": "the whole call: numpy restatement of matrix_blas_lapack.rs:1710-1932 over OpenBLAS"}
+        res["fp64"]["max_rel_err_vs_oracle"] = float(np.abs(outs["fp64"].cpu().numpy().reshape(n, n, order="F") - Xo).max()
+                                                     / np.abs(Xo).max())
+    del outs, S, Q
+    torch.cuda.empty_cache()
+    return res
+
+
 # ------------------------------------------------------------- layout utilities --
 def layout_leg(args, rt, torch, stream, B):
     """RIFull transposes and the symmetric pair packing on this workload's ri3ao
@@ -691,6 +749,7 @@ def main():
     if args.ri3fn:
         ri3fn = ri3fn_leg(args, rt, torch, stream, B)
         ri3fn["layout"] = layout_leg(args, rt, torch, stream, B)
+        ri3fn["newton_schulz"] = newton_schulz_leg(args, rt, torch, stream)
 
     batched = None
     if args.batch_mols > 0:

@@ -200,6 +200,26 @@ rt_status rt_ri_j(const double* B, const double* D, int nb, int naux, double* w,
  * float64 with a fixed-order tree.  Writes one double to ex_device. */
 rt_status rt_ri_exchange_energy(const double* D, const double* K, int nb, double* ex_device, void* stream);
 
+/* Inverse square root of a symmetric positive matrix by Newton-Schulz
+ * iteration, _newton_schulz_inverse_square_root_v02
+ * (src/matrix/matrix_blas_lapack.rs:1710-1778) with its per-stage iteration
+ * _newton_schulz_inverse_square_root_lf (:1780-1932): the matrix is
+ * normalised by its Frobenius norm; for each level shift in turn,
+ *   X <- 0.5 X (3I - A X X)
+ * runs from the previous stage's result until ||X_next - X||_F / n^2 <=
+ * threshold, with the reference's mixing branches; a stage that fails is
+ * retried with the mixing parameter halved (at most six times), after which
+ * the stages stop.  The result is rescaled by ||S||_F^-1/2 into out[n, n].
+ * S and out are device pointers; level_shift (n_level_shift >= 1 entries) is
+ * host memory.  converged (may be NULL) receives the reference's flag; steps
+ * (may be NULL) the number of X_next evaluations over all stages and retries
+ * (three n x n products each).  form
+ * RT_FORM_FP64, or RT_FORM_SPLIT (nslices 3..8) for the three products of a
+ * step.  Synchronises `stream` once per step (the branches depend on norms). */
+rt_status rt_newton_schulz_inv_sqrt(const double* S, int n, double threshold, double mix_parameter, int num_iter,
+                                    const double* level_shift, int n_level_shift, int form, int nslices,
+                                    double* out, int* converged, int* steps, void* stream);
+
 /* ------------------------------------------------------------------------
  * Layout utilities (device pointers).  Blocks are given by 0-based starts
  * and lengths; a source and target that share memory behave as a Fortran

@@ -312,6 +312,117 @@ def rifull_to_matfull_symm(data, nao, naux):
 
 
 # --------------------------------------------------------------------------
+# Newton-Schulz inverse square root (src/matrix/matrix_blas_lapack.rs:1710-1932)
+# --------------------------------------------------------------------------
+def newton_schulz_lf(input_matr, initial_guess, threshold, mix_parameter, level_shift, num_iter):
+    """_newton_schulz_inverse_square_root_lf (matrix_blas_lapack.rs:1780-1932), step by step.
+
+    X_next = 0.5 X (3I - A X X); the mixing branches, the level shift on
+    diagonal elements above the threshold and the returned iterate (the last
+    X_next, not the mixed X) follow the reference.  Returns
+    (matrix, n_singular = 0, converged, evals), where evals counts the X_next
+    evaluations (three products each).
+    """
+    a = np.array(input_matr, dtype=np.float64, order="F")
+    n = a.shape[0]
+    num_elems = a.size
+    unit = 3.0 * np.eye(n)
+    matr = a.copy(order="F")
+    d = np.diag(matr).copy()
+    d = np.where(d > threshold, d + level_shift, 0.0)
+    matr[np.arange(n), np.arange(n)] = d
+    trace_1 = float(np.sum(np.diag(matr))) / n
+    initial_a = 1.0 / np.sqrt(trace_1)
+    if initial_guess is not None:
+        x = np.array(initial_guess, dtype=np.float64, order="F")
+    else:
+        x = np.zeros((n, n), order="F")
+        x[np.arange(n), np.arange(n)] = np.where(np.abs(np.diag(matr)) < threshold, 0.0, initial_a)
+
+    def step(x):
+        t = matr @ x
+        w = t @ x
+        u = unit + w * -1.0
+        return 0.5 * (x @ u)
+
+    nxt = step(x)
+    evals = 1
+    norm = np.sqrt(np.sum((x - nxt) ** 2)) / num_elems
+    prev_norm = norm
+    x = nxt.copy()
+    converged = bool(norm <= threshold)
+    count_unchanged = 0
+    for _ in range(num_iter):
+        nxt = step(x)
+        evals += 1
+        norm = np.sqrt(np.sum((x - nxt) ** 2)) / num_elems
+        converged = bool(norm <= threshold)
+        change_norm = norm - prev_norm
+        prev_norm = norm
+        prev = x.copy()
+        if converged:
+            break
+        if norm <= threshold * 10.0:
+            x = mix_parameter * nxt + (1.0 - mix_parameter) * x
+            x = mix_parameter * prev + (1.0 - mix_parameter) * x
+            count_unchanged = 0
+        elif change_norm > threshold:
+            count_unchanged = 0
+            x = mix_parameter * nxt + (1.0 - mix_parameter) * x
+            tmp = np.sqrt(np.sum(x ** 2))
+            if tmp >= 100.0:
+                x = x / tmp
+                x = x / tmp
+                x[np.arange(n), np.arange(n)] *= tmp
+        elif abs(change_norm) <= threshold:
+            if count_unchanged < 5:
+                x = mix_parameter * nxt + (1.0 - mix_parameter) * x
+                count_unchanged += 1
+            else:
+                x[np.arange(n), np.arange(n)] = initial_a
+                count_unchanged = 0
+        else:
+            x = nxt.copy()
+            count_unchanged = 0
+    return np.asfortranarray(nxt), 0, converged, evals
+
+
+def newton_schulz_inverse_square_root_v02(original_matr, threshold, mix_parameter, num_iter, level_shift):
+    """_newton_schulz_inverse_square_root_v02 (matrix_blas_lapack.rs:1710-1778): normalise by the
+    Frobenius norm, run the level-shift sequence (halving the mixing parameter up to six times when a
+    stage fails, then stopping), rescale by norm^-1/2.  Returns (matrix, 0, converged, total_evals)."""
+    if len(level_shift) == 0:
+        raise ValueError("level_shift must not be empty (the reference unwraps a None guess)")
+    a = np.array(original_matr, dtype=np.float64, order="F")
+    original_norm = float(np.sqrt(np.sum(a ** 2)))
+    matr_0 = a / original_norm
+    guess = None
+    converged = False
+    total = 0
+    for shift in level_shift:
+        out, _, lf_conv, steps = newton_schulz_lf(matr_0, guess, threshold, mix_parameter, shift, num_iter)
+        total += steps
+        fine_mix = mix_parameter
+        if not lf_conv:
+            lf2 = lf_conv
+            cur = 0
+            while not lf2:
+                fine_mix = fine_mix / 2.0
+                cur += 1
+                out, _, lf2, steps = newton_schulz_lf(matr_0, guess, threshold, fine_mix, shift, num_iter)
+                total += steps
+                if cur > 5:
+                    break
+            guess = out
+            converged = lf2
+            break
+        converged = lf_conv
+        guess = out
+    res = guess * original_norm ** -0.5
+    return np.asfortranarray(res), 0, converged, total
+
+
+# --------------------------------------------------------------------------
 # Synthetic inputs
 # --------------------------------------------------------------------------
 def synth_ri3ao(seed, nb, naux, P0=0, P1=None):

@@ -147,6 +147,9 @@ def lib() -> ctypes.CDLL:
     L.rt_ri_pack_symm.restype = c_int
     L.rt_ri_pack_symm.argtypes = [vp, c_int, c_int, vp, vp]
     L.special_dgemm_f_01_.restype = None
+    L.rt_newton_schulz_inv_sqrt.restype = c_int
+    L.rt_newton_schulz_inv_sqrt.argtypes = [vp, c_int, c_dbl, c_dbl, c_int, ctypes.POINTER(c_dbl), c_int, c_int, c_int,
+                                            vp, ctypes.POINTER(c_int), ctypes.POINTER(c_int), vp]
     L.ri_ao2mo_f_.restype = None
     L.general_dgemm_f_.restype = None
     _lib = L
@@ -466,6 +469,26 @@ def ri_pack_symm(ri, nao: int, naux: int, out=None, stream=None):
         out = torch.empty(max(nao * (nao + 1) // 2 * naux, 1), dtype=torch.float64, device=ri.device)
     _check(lib().rt_ri_pack_symm(_dptr(ri), nao, naux, _dptr(out), _stream(stream)))
     return out[: nao * (nao + 1) // 2 * naux]
+
+
+def newton_schulz_inverse_square_root_v02(S, n: int, threshold: float, mix_parameter: float, num_iter: int,
+                                          level_shift, form: str = "fp64", nslices: int = DEFAULT_NSLICES,
+                                          out=None, stream=None):
+    """_newton_schulz_inverse_square_root_v02 (src/matrix/matrix_blas_lapack.rs:1710-1778) on a device
+    [n, n] matrix.  Returns (matrix, n_singular = 0, converged) like the reference, plus the number of
+    X_next evaluations (three n x n products each)."""
+    import torch
+
+    if len(level_shift) == 0:
+        raise ValueError("level_shift must not be empty")
+    if out is None:
+        out = torch.empty(n * n, dtype=torch.float64, device=S.device)
+    shifts = (ctypes.c_double * len(level_shift))(*[float(x) for x in level_shift])
+    conv, steps = ctypes.c_int(0), ctypes.c_int(0)
+    _check(lib().rt_newton_schulz_inv_sqrt(_dptr(S), n, threshold, mix_parameter, num_iter, shifts,
+                                           len(level_shift), _form(form), nslices, _dptr(out), ctypes.byref(conv),
+                                           ctypes.byref(steps), _stream(stream)))
+    return out, 0, bool(conv.value), int(steps.value)
 
 
 def ri_j(B, D, nb: int, naux: int, w=None, J=None, stream=None):
