@@ -378,7 +378,21 @@ def ri3fn_leg(args, rt, torch, stream, B):
     split_vs_fp64 = float((T - T64).abs().max() / T64.abs().max())
     del T, T64
     torch.cuda.empty_cache()
-    res = {"shape": {"ten3_a": list(size_a), "matr_b": list(size_b)}, "flop": fl,
+    # The drop-in symbol on pageable host memory (what a Rust Vec is): transfers inside the timing.
+    ny = NB // 10
+    th = np.ascontiguousarray(Bv[:, :ny, :].cpu().numpy())  # [P][nu < ny][mu] = ten3_a [NB, ny, NAUX]
+    th = th.reshape(-1)
+    t0 = time.perf_counter()
+    rt.special_dgemm_f_01(th, (NB, ny, NAUX), range(NB), 0, range(NAUX), Mh.reshape(-1, order="F"), size_b,
+                          range(NAUX), range(NAUX), 1.0, 0.0)
+    dt_h = time.perf_counter() - t0
+    fl_h = 2.0 * NB * ny * NAUX * NAUX
+    e2e_dropin = {"tflops": fl_h / dt_h / 1e12, "ms": dt_h * 1e3, "h2d_bytes": 8 * NB * ny * NAUX + 8 * NAUX * NAUX,
+                  "d2h_bytes": 8 * NB * ny * NAUX,
+                  "sample": f"special_dgemm_f_01_ (float64 form) on a pageable [{NB}, {ny}, {NAUX}] host tensor, "
+                            f"copies in and out inside the timing"}
+    del th
+    res = {"shape": {"ten3_a": list(size_a), "matr_b": list(size_b)}, "flop": fl, "e2e_dropin": e2e_dropin,
            "split": {"ms": ms_sp, "tflops": fl / ms_sp / 1e9},
            "fp64": {"ms": ms_64, "tflops": fl / ms_64 / 1e9}, "speedup_vs_fp64": ms_64 / ms_sp,
            "max_rel_err_vs_oracle": errs, "split_vs_fp64_max_rel": split_vs_fp64,
@@ -486,6 +500,11 @@ def layout_leg(args, rt, torch, stream, B):
         ms = timed(lambda: rt.ri_transpose(B, (NB, NB, NAUX), order, out=out, stream=stream))
         gbs = 16.0 * nel / ms / 1e6
         res["transpose_" + order] = {"ms": ms, "gbs": gbs, "frac_of_copy": gbs / hbm}
+    half = NAUX // 2
+    ms = timed(lambda: rt.copy_rr((NB, NB, half), B, (NB, NB, NAUX), (0, 0, half), out, (NB, NB, NAUX), (0, 0, 0),
+                                  stream=stream))
+    gbs = 16.0 * NB * NB * half / ms / 1e6
+    res["copy_rr_half"] = {"ms": ms, "gbs": gbs, "frac_of_copy": gbs / hbm}
     npair = NB * (NB + 1) // 2
     ms = timed(lambda: rt.ri_pack_symm(B, NB, NAUX, out=out, stream=stream))
     gbs = 16.0 * npair * NAUX / ms / 1e6
