@@ -73,6 +73,38 @@ __global__ void axpy_dev_kernel(double* __restrict__ x, const double* __restrict
         x[i] = fma(-a, q[i], x[i]);
 }
 
+// Column dots, several at once: partial[k * gridDim.x + b] = this block's share of
+// sum_i A[i + k lda] * Bm[i + k ldb] for column k = blockIdx.y (lda = 0: one vector A
+// against every column of Bm).  Fixed-order reduction, like dot_partial_kernel.
+__global__ void __launch_bounds__(256) coldot_partial_kernel(const double* __restrict__ A, int64_t lda,
+                                                             const double* __restrict__ Bm, int64_t ldb, int64_t n,
+                                                             double* __restrict__ partial) {
+    __shared__ double red[8];
+    const int k = blockIdx.y;
+    const double* a = A + (int64_t)k * lda;
+    const double* b = Bm + (int64_t)k * ldb;
+    double s = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        s = fma(a[i], b[i], s);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double t = threadIdx.x < 8 ? red[threadIdx.x] : 0.0;
+        for (int o = 4; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (threadIdx.x == 0) partial[(int64_t)k * gridDim.x + blockIdx.x] = t;
+    }
+}
+
+// X[:, k] -= c[k] * q for the nv columns of X (leading dimension ld).
+__global__ void multi_axpy_kernel(double* __restrict__ X, int64_t ld, int nv, const double* __restrict__ q,
+                                  const double* __restrict__ c, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double qi = q[i];
+        for (int k = 0; k < nv; ++k) X[i + k * ld] = fma(-c[k], qi, X[i + k * ld]);
+    }
+}
+
 // y = x / s  (host scalar; division as in the reference's `x /= norm`)
 __global__ void div_kernel(double* __restrict__ y, const double* __restrict__ x, double s, int64_t n) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -152,6 +184,51 @@ struct VecOps {
     }
     rt_status copy(double* y, const double* x, int64_t n) {
         RT_CUDA_TRY(cudaMemcpyAsync(y, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+        return RT_OK;
+    }
+    // out_dev[k] = A[:, k] . Bm[:, k] for k < nv (lda = 0: the single vector A), each
+    // reduced in a fixed order over kColBlocks partial sums.
+    static constexpr int kColBlocks = 64;
+    double* colpart = nullptr;  // kMaxCols * kColBlocks
+    double* colout = nullptr;   // max(kMaxCols, ncolout) entries
+    int ncolout = 0;
+    static constexpr int kMaxCols = 64;
+    rt_status coldots(const double* A, int64_t lda, const double* Bm, int64_t ldb, int nv, int64_t n,
+                      double* out_dev) {
+        for (int k0 = 0; k0 < nv; k0 += kMaxCols) {
+            const int m = std::min(kMaxCols, nv - k0);
+            coldot_partial_kernel<<<dim3(kColBlocks, m), 256, 0, s>>>(A + k0 * lda, lda, Bm + k0 * ldb, ldb, n,
+                                                                      colpart);
+            RT_TRY(check_launch("coldot_partial_kernel"));
+            for (int k = 0; k < m; ++k) {
+                dot_final_kernel<<<1, kRedBlocks, 0, s>>>(colpart + (int64_t)k * kColBlocks, kColBlocks,
+                                                          out_dev + k0 + k);
+                RT_TRY(check_launch("dot_final_kernel"));
+            }
+        }
+        return RT_OK;
+    }
+    // Euclidean norms of the nv columns of X, read back with one synchronisation.
+    rt_status norms_host(const double* X, int64_t ld, int nv, int64_t n, double* out) {
+        if (nv <= 0) return RT_OK;
+        RT_REQUIRE(nv <= ncolout, "rt_davidson_solve: too many columns for one norm batch");
+        RT_TRY(coldots(X, ld, X, ld, nv, n, colout));
+        std::vector<double> d(nv);
+        RT_CUDA_TRY(cudaMemcpyAsync(d.data(), colout, sizeof(double) * nv, cudaMemcpyDeviceToHost, s));
+        RT_CUDA_TRY(cudaStreamSynchronize(s));
+        for (int k = 0; k < nv; ++k) out[k] = sqrt(d[k]);
+        return RT_OK;
+    }
+    // X[:, k] -= (q . X[:, k]) q for k < nv: one modified Gram-Schmidt step of q
+    // applied to every column, the coefficients kept on the device.
+    rt_status project_out_many(double* X, int64_t ld, int nv, const double* q, int64_t n) {
+        if (nv <= 0) return RT_OK;
+        for (int k0 = 0; k0 < nv; k0 += kMaxCols) {
+            const int m = std::min(kMaxCols, nv - k0);
+            RT_TRY(coldots(q, 0, X + k0 * ld, ld, m, n, colout));
+            multi_axpy_kernel<<<grid, 256, 0, s>>>(X + k0 * ld, ld, m, q, colout, n);
+            RT_TRY(check_launch("multi_axpy_kernel"));
+        }
         return RT_OK;
     }
 };
@@ -259,6 +336,14 @@ rt_status rt_davidson_solve(rt_matvec_fn a_x, void* ctx, const double* x0_1d, co
     };
     VecOps ops{s, red.as<double>(), red.as<double>() + kRedBlocks, std::min<int>(4 * sm_count(), (int)ceil_div(n, 256))};
     if (ops.grid < 1) ops.grid = 1;
+    ScratchBuf colb, gb;
+    ops.ncolout = std::max(cap, (int)VecOps::kMaxCols);
+    RT_TRY(scratch_alloc(colb, sizeof(double) * (size_t)(VecOps::kMaxCols * VecOps::kColBlocks + ops.ncolout), s));
+    ops.colpart = colb.as<double>();
+    ops.colout = ops.colpart + VecOps::kMaxCols * VecOps::kColBlocks;
+    // X_new^T AX for fill_heff, at most cap x cap
+    RT_TRY(scratch_alloc(gb, sizeof(double) * (size_t)cap * cap, s));
+    std::vector<double> ghost((size_t)cap * cap);
     auto col = [&](double* base, int j) { return base + (size_t)j * n; };
 
     // Modified Gram-Schmidt of the columns of src (count m) into dst; returns the kept count.
@@ -339,17 +424,19 @@ rt_status rt_davidson_solve(rt_matvec_fn a_x, void* ctx, const double* x0_1d, co
             if (!fresh)
                 for (int j = 0; j < head; ++j)
                     for (int i = 0; i < head; ++i) hn[(size_t)j * space + i] = heff[(size_t)j * head + i];
-            for (int i = row0; i < row1; ++i)
-                for (int j = row0; j < row1; ++j) {
-                    double v = 0.0;
-                    RT_TRY(ops.dot_host(col(XS, i), col(AXs, j), n, &v));
-                    hn[(size_t)j * space + i] = v;
-                    hn[(size_t)i * space + j] = v;
-                }
-            for (int j = row0; j < row1; ++j)
-                for (int i = 0; i < row0; ++i) {
-                    double v = 0.0;
-                    RT_TRY(ops.dot_host(col(AXs, i), col(XS, j), n, &v));
+            // The reference's loops (davidson.rs:345-380) leave H(i, j) = x_max(i,j) . ax_min(i,j)
+            // for every pair with a new index; all of those are entries of
+            // G = X_new^T AX[:, 0:space], formed by one GEMM and read back once.
+            const int nnewc = row1 - row0;
+            RT_TRY(rt_dgemm('T', 'N', nnewc, space, (int)n, 1.0, col(XS, row0), (int)n, AXs, (int)n, 0.0,
+                            gb.as<double>(), nnewc, s));
+            RT_CUDA_TRY(cudaMemcpyAsync(ghost.data(), gb.p, sizeof(double) * (size_t)nnewc * space,
+                                        cudaMemcpyDeviceToHost, s));
+            RT_CUDA_TRY(cudaStreamSynchronize(s));
+            auto G = [&](int a, int b) { return ghost[(size_t)b * nnewc + (a - row0)]; };  // x_a . ax_b, a new
+            for (int i = 0; i < row1; ++i)
+                for (int j = std::max(i, row0); j < row1; ++j) {
+                    const double v = G(j, i);  // j = max(i, j) is new
                     hn[(size_t)j * space + i] = v;
                     hn[(size_t)i * space + j] = v;
                 }
@@ -372,9 +459,9 @@ rt_status rt_davidson_solve(rt_matvec_fn a_x, void* ctx, const double* x0_1d, co
             de[k] = k < (int)elast.size() ? ev[k] - elast[k] : ev[k];
             residual_kernel<<<ops.grid, 256, 0, s>>>(col(XT, k), col(AX0, k), col(X0, k), ev[k], n);
             RT_TRY(check_launch("residual_kernel"));
-            RT_TRY(ops.norm_host(col(XT, k), n, &dxn[k]));
-            convv[k] = fabs(de[k]) < tol && dxn[k] < sqrt(tol);
         }
+        RT_TRY(ops.norms_host(XT, n, nroots_current, n, dxn.data()));
+        for (int k = 0; k < nroots_current; ++k) convv[k] = fabs(de[k]) < tol && dxn[k] < sqrt(tol);
         for (int k = 0; k < nroots; ++k) all_conv = all_conv && convv[k];
         const double max_dx = *std::max_element(dxn.begin(), dxn.end());
         if (print_level > 0)
@@ -390,6 +477,8 @@ rt_status rt_davidson_solve(rt_matvec_fn a_x, void* ctx, const double* x0_1d, co
             continue;
         }
         // Precondition, normalise and project the residuals (davidson.rs:222-245).
+        // Each vector's steps depend only on that vector, so the norms of a phase are
+        // formed together and read back with one synchronisation.
         int nnew = 0;
         for (int k = 0; k < nroots_current; ++k) {
             if (dxn[k] * dxn[k] > lindep) {
@@ -397,18 +486,19 @@ rt_status rt_davidson_solve(rt_matvec_fn a_x, void* ctx, const double* x0_1d, co
                 if (t != col(XT, k)) RT_TRY(ops.copy(t, col(XT, k), n));
                 precond_kernel<<<ops.grid, 256, 0, s>>>(t, hdiag, ev[0], n);
                 RT_TRY(check_launch("precond_kernel"));
-                double norm = 0.0;
-                RT_TRY(ops.norm_host(t, n, &norm));
-                RT_TRY(ops.divide(t, t, norm, n));
                 ++nnew;
             }
         }
-        for (int i = 0; i < space; ++i)
-            for (int k = 0; k < nnew; ++k) RT_TRY(ops.project_out(col(XT, k), col(XS, i), n));
+        std::vector<double> nrm(std::max(nnew, 1));
+        RT_TRY(ops.norms_host(XT, n, nnew, n, nrm.data()));
+        for (int k = 0; k < nnew; ++k) RT_TRY(ops.divide(col(XT, k), col(XT, k), nrm[k], n));
+        // Modified Gram-Schmidt against the subspace, in the reference's order
+        // (subspace vector i outer, new vectors inner).
+        for (int i = 0; i < space; ++i) RT_TRY(ops.project_out_many(XT, n, nnew, col(XS, i), n));
+        RT_TRY(ops.norms_host(XT, n, nnew, n, nrm.data()));
         int kept = 0;
         for (int k = 0; k < nnew; ++k) {
-            double norm = 0.0;
-            RT_TRY(ops.norm_host(col(XT, k), n, &norm));
+            const double norm = nrm[k];
             if (norm * norm > lindep) {
                 RT_TRY(ops.divide(col(XT, kept), col(XT, k), norm, n));
                 ++kept;
