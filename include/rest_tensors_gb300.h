@@ -367,6 +367,11 @@ rt_status rt_profile_get(int kind, double* total_ms, long long* launches, double
 rt_status rt_debug_fail_alloc_after(long long n);
 rt_status rt_debug_wait_timeout(long long cycles, void* stream);
 rt_status rt_debug_chunk_bytes(long long bytes);
+/* rt_debug_symeig(n, a, w, z): the Davidson subspace eigensolver on a host
+ * column-major symmetric matrix a[n, n]: eigenvalues ascending in w[n],
+ * eigenvectors in the columns of z[n, n], each with its largest-magnitude
+ * component positive.  Host code only; callable without a GPU. */
+rt_status rt_debug_symeig(int n, const double* a, double* w, double* z);
 
 #ifdef __cplusplus
 }
