@@ -259,13 +259,13 @@ __global__ void __launch_bounds__(256) slice_strided_kernel(SliceArgs a) {
 constexpr int kFusedRows = 16;    // contiguous-row slicer
 constexpr int kStridedRows = 16;  // strided-row slicer (8 rows at 3 CTAs/SM measured slower)
 template <int S, int NBLK, int RR>
-__global__ void __launch_bounds__(256, RR >= 16 ? 2 : 3)
-    slice_strided_rowmax_kernel(SliceArgs a, int* __restrict__ emax_out) {
+__device__ __forceinline__ void slice_strided_rowmax_body(const SliceArgs& a, int* __restrict__ emax_out,
+                                                          int64_t blk) {
     constexpr int KQN = 256 / RR;
     __shared__ unsigned int red[8][RR];
     const int r = threadIdx.x % RR;
     const int kq = threadIdx.x / RR;
-    const int64_t row = (int64_t)blockIdx.x * RR + r;
+    const int64_t row = blk * RR + r;
     const bool valid = row < a.src.rows;
     const double* base = valid ? a.src.p + (row % a.src.div) * a.src.s0 + (row / a.src.div) * a.src.s1 : nullptr;
     double x[NBLK][8];
@@ -310,6 +310,12 @@ __global__ void __launch_bounds__(256, RR >= 16 ? 2 : 3)
     }
 }
 
+template <int S, int NBLK, int RR>
+__global__ void __launch_bounds__(256, RR >= 16 ? 2 : 3)
+    slice_strided_rowmax_kernel(SliceArgs a, int* __restrict__ emax_out) {
+    slice_strided_rowmax_body<S, NBLK, RR>(a, emax_out, blockIdx.x);
+}
+
 // Contiguous rows (sk == 1) with a short contraction (K <= 128 * NBLK): row
 // exponents and digits in one pass.  A CTA covers 16 rows.  Warp w handles rows
 // 8 (w & 1) .. + 7 (lane & 7) and k-groups 4 (w >> 1) + (lane >> 3); each thread
@@ -317,12 +323,13 @@ __global__ void __launch_bounds__(256, RR >= 16 ? 2 : 3)
 // threads of a row (4 lanes x 4 warps) reduce its exponent maximum; then every
 // thread slices its runs.  Stores of one instruction cover 8 rows x 16 bytes.
 template <int S, int NBLK>
-__global__ void __launch_bounds__(256, 2) slice_contig_rowmax_kernel(SliceArgs a, int* __restrict__ emax_out) {
+__device__ __forceinline__ void slice_contig_rowmax_body(const SliceArgs& a, int* __restrict__ emax_out,
+                                                         int64_t blk) {
     __shared__ unsigned int red[4][kFusedRows];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int r = 8 * (warp & 1) + (lane & 7);
     const int kq = 4 * (warp >> 1) + (lane >> 3);  // 0..15
-    const int64_t row = (int64_t)blockIdx.x * kFusedRows + r;
+    const int64_t row = blk * kFusedRows + r;
     const bool valid = row < a.src.rows;
     const double* base = valid ? a.src.p + (row % a.src.div) * a.src.s0 + (row / a.src.div) * a.src.s1 : nullptr;
     double x[NBLK][8];
@@ -362,6 +369,41 @@ __global__ void __launch_bounds__(256, 2) slice_contig_rowmax_kernel(SliceArgs a
         digits8<S>(x[j], (int)m, w);
         store8<S>(a, tile, k0 / KB, rt_, (int)(k0 & (KB - 1)), w);
     }
+}
+
+template <int S, int NBLK>
+__global__ void __launch_bounds__(256, 2) slice_contig_rowmax_kernel(SliceArgs a, int* __restrict__ emax_out) {
+    slice_contig_rowmax_body<S, NBLK>(a, emax_out, blockIdx.x);
+}
+
+// One-pass slicing of many operands in one launch (the batched products): block
+// b belongs to job p with prefix[p] <= b < prefix[p + 1] and runs that job's
+// block b - prefix[p].
+constexpr int kMaxSliceGroup = 48;
+struct SliceGroup {
+    SliceArgs a[kMaxSliceGroup];
+    int* emax[kMaxSliceGroup];
+    int64_t prefix[kMaxSliceGroup + 1];
+    int count;
+};
+
+__device__ __forceinline__ int slice_job(const SliceGroup& G, int64_t b) {
+    int p = 0;
+    while (p + 1 < G.count && b >= G.prefix[p + 1]) ++p;
+    return p;
+}
+
+template <int S, int NBLK, int RR>
+__global__ void __launch_bounds__(256, RR >= 16 ? 2 : 3)
+    slice_strided_rowmax_grouped(const __grid_constant__ SliceGroup G) {
+    const int p = slice_job(G, blockIdx.x);
+    slice_strided_rowmax_body<S, NBLK, RR>(G.a[p], G.emax[p], (int64_t)blockIdx.x - G.prefix[p]);
+}
+
+template <int S, int NBLK>
+__global__ void __launch_bounds__(256, 2) slice_contig_rowmax_grouped(const __grid_constant__ SliceGroup G) {
+    const int p = slice_job(G, blockIdx.x);
+    slice_contig_rowmax_body<S, NBLK>(G.a[p], G.emax[p], (int64_t)blockIdx.x - G.prefix[p]);
 }
 
 // Contiguous rows (sk == 1): the [T x 32] tile is staged through shared
@@ -875,8 +917,75 @@ rt_status row_exponents(const Operand& op, int64_t K, int* emax, cudaStream_t st
     return check_launch("emax_strided_kernel");
 }
 
+// One-pass slicing jobs collected by the grouped path and launched together.
+struct SliceJob {
+    int kind;   // 0: contiguous rows, 1: strided rows
+    int nblk;   // the kernel's NBLK
+    SliceArgs sa;
+    int* emax;
+    int64_t blocks;
+};
+struct SliceQueue {
+    std::vector<SliceJob> jobs;
+};
+
 template <int S>
-rt_status slice_operand(const Operand& op, int64_t K, int T, Sliced& out, cudaStream_t stream) {
+rt_status launch_slice_group(int kind, int nblk, const SliceGroup& G, unsigned grid, cudaStream_t stream) {
+    constexpr int RR = kStridedRows, KQN = 256 / RR;
+    if (kind == 0) {
+        switch (nblk) {
+            case 1: slice_contig_rowmax_grouped<S, 1><<<grid, 256, 0, stream>>>(G); break;
+            case 2: slice_contig_rowmax_grouped<S, 2><<<grid, 256, 0, stream>>>(G); break;
+            case 3: slice_contig_rowmax_grouped<S, 3><<<grid, 256, 0, stream>>>(G); break;
+            case 4: slice_contig_rowmax_grouped<S, 4><<<grid, 256, 0, stream>>>(G); break;
+            default: slice_contig_rowmax_grouped<S, 5><<<grid, 256, 0, stream>>>(G); break;
+        }
+        return check_launch("slice_contig_rowmax_grouped");
+    }
+    switch (nblk) {
+        case 1: slice_strided_rowmax_grouped<S, 1, RR><<<grid, 256, 0, stream>>>(G); break;
+        case 2: slice_strided_rowmax_grouped<S, 2, RR><<<grid, 256, 0, stream>>>(G); break;
+        case 3: slice_strided_rowmax_grouped<S, 3, RR><<<grid, 256, 0, stream>>>(G); break;
+        case 4: slice_strided_rowmax_grouped<S, 4, RR><<<grid, 256, 0, stream>>>(G); break;
+        default: slice_strided_rowmax_grouped<S, (640 + 8 * KQN - 1) / (8 * KQN), RR><<<grid, 256, 0, stream>>>(G);
+            break;
+    }
+    return check_launch("slice_strided_rowmax_grouped");
+}
+
+// Launch the queued jobs: one grouped launch per (kind, NBLK) and per 48 jobs.
+template <int S>
+rt_status flush_slices(SliceQueue& q, cudaStream_t stream) {
+    std::vector<bool> done(q.jobs.size(), false);
+    for (size_t i = 0; i < q.jobs.size(); ++i) {
+        if (done[i]) continue;
+        const int kind = q.jobs[i].kind, nblk = q.jobs[i].nblk;
+        SliceGroup G{};
+        G.count = 0;
+        G.prefix[0] = 0;
+        for (size_t j = i; j < q.jobs.size(); ++j) {
+            if (done[j] || q.jobs[j].kind != kind || q.jobs[j].nblk != nblk) continue;
+            G.a[G.count] = q.jobs[j].sa;
+            G.emax[G.count] = q.jobs[j].emax;
+            G.prefix[G.count + 1] = G.prefix[G.count] + q.jobs[j].blocks;
+            ++G.count;
+            done[j] = true;
+            if (G.count == kMaxSliceGroup) {
+                RT_TRY(launch_slice_group<S>(kind, nblk, G, (unsigned)G.prefix[G.count], stream));
+                G.count = 0;
+            }
+        }
+        if (G.count > 0) RT_TRY(launch_slice_group<S>(kind, nblk, G, (unsigned)G.prefix[G.count], stream));
+    }
+    q.jobs.clear();
+    return RT_OK;
+}
+
+// Digit planes of one operand.  With a queue, the one-pass cases are recorded
+// there (their planes allocated now) and launched later by flush_slices.
+template <int S>
+rt_status slice_operand(const Operand& op, int64_t K, int T, Sliced& out, cudaStream_t stream,
+                        SliceQueue* queue = nullptr) {
     out.T = T;
     out.tiles = ceil_div(op.rows, T);
     out.Kb = ceil_div(K, KB);
@@ -890,6 +999,11 @@ rt_status slice_operand(const Operand& op, int64_t K, int T, Sliced& out, cudaSt
     sa.out = out.planes.as<uint16_t>(); sa.emax = out.emax.as<int>(); sa.err = err;
     if (op.sk == 1 && out.Kb * KB <= 128 * 5) {
         const unsigned grid = (unsigned)(out.tiles * T / kFusedRows);
+        if (queue) {
+            queue->jobs.push_back(SliceJob{0, (int)std::min<int64_t>(ceil_div(out.Kb, 8), 5), sa, out.emax.as<int>(),
+                                           (int64_t)grid});
+            return RT_OK;
+        }
         switch ((int)ceil_div(out.Kb, 8)) {
             case 1: slice_contig_rowmax_kernel<S, 1><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
             case 2: slice_contig_rowmax_kernel<S, 2><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
@@ -908,6 +1022,11 @@ rt_status slice_operand(const Operand& op, int64_t K, int T, Sliced& out, cudaSt
     } else if (op.s0 == 1 && out.Kb * KB <= 640) {
         constexpr int RR = kStridedRows, KQN = 256 / RR;
         const unsigned grid = (unsigned)(out.tiles * T / RR);
+        if (queue) {
+            const int nb = (int)ceil_div(out.Kb * KB, 8 * KQN);
+            queue->jobs.push_back(SliceJob{1, nb <= 4 ? nb : 5, sa, out.emax.as<int>(), (int64_t)grid});
+            return RT_OK;
+        }
         switch ((int)ceil_div(out.Kb * KB, 8 * KQN)) {
             case 1: slice_strided_rowmax_kernel<S, 1, RR><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
             case 2: slice_strided_rowmax_kernel<S, 2, RR><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
@@ -944,6 +1063,7 @@ struct Prepared {
     int64_t active = 0;   // output tiles that carry work (upper triangle when symmetric)
     int chunks_per_item = 0;
     double flops = 0.0;   // algorithmic digit-pair tensor work
+    double slice_bytes = 0.0;
 };
 
 template <int S>
@@ -958,7 +1078,7 @@ void ensure_attrs() {
 // Slicing and argument set-up for one product; the GEMM itself is launched by
 // launch_group, possibly together with other products.
 template <int S>
-rt_status prepare(const OzGemm& g, Prepared& P, cudaStream_t stream) {
+rt_status prepare(const OzGemm& g, Prepared& P, cudaStream_t stream, SliceQueue* queue = nullptr) {
     ensure_attrs<S>();
     Operand A{g.A.p, g.A.rows, g.A.div, g.A.s0, g.A.s1, g.A.sk};
     Operand B{g.B.p, g.B.rows, g.B.div, g.B.s0, g.B.s1, g.B.sk};
@@ -971,7 +1091,8 @@ rt_status prepare(const OzGemm& g, Prepared& P, cudaStream_t stream) {
     // fused path only reads A's float64 once for its row exponents).
     const double slice_bytes = fused ? (double)A.rows * g.K * 8.0 + (double)B.rows * g.K * (8.0 + 2.0 * S)
                                      : (double)(A.rows + (reuse ? 0 : B.rows)) * (double)g.K * (8.0 + 2.0 * S);
-    prof_begin(PROF_OZ_SLICE, stream);
+    // With a queue, the caller times the grouped slicing itself.
+    if (!queue) prof_begin(PROF_OZ_SLICE, stream);
     if (fused) {
         sa.T = TM;
         sa.tiles = ceil_div(A.rows, TM);
@@ -979,10 +1100,11 @@ rt_status prepare(const OzGemm& g, Prepared& P, cudaStream_t stream) {
         RT_TRY(scratch_alloc(sa.emax, sizeof(int) * (size_t)A.rows, stream));
         RT_TRY(row_exponents<S>(A, g.K, sa.emax.as<int>(), stream));
     } else {
-        RT_TRY(slice_operand<S>(A, g.K, TM, sa, stream));
+        RT_TRY(slice_operand<S>(A, g.K, TM, sa, stream, queue));
     }
-    if (!reuse) RT_TRY(slice_operand<S>(B, g.K, TN, sb, stream));
-    prof_end(PROF_OZ_SLICE, stream, slice_bytes);
+    if (!reuse) RT_TRY(slice_operand<S>(B, g.K, TN, sb, stream, queue));
+    if (!queue) prof_end(PROF_OZ_SLICE, stream, slice_bytes);
+    P.slice_bytes = slice_bytes;
 
     GemmArgs& a = P.a;
     if (fused) {
@@ -1131,10 +1253,16 @@ template <int S>
 rt_status run_many(const OzGemm* gs, int n, cudaStream_t stream) {
     std::vector<Prepared> P(n);
     int64_t active = 0;
+    SliceQueue queue;
+    double slice_bytes = 0.0;
+    prof_begin(PROF_OZ_SLICE, stream);
     for (int i = 0; i < n; ++i) {
-        RT_TRY(prepare<S>(gs[i], P[i], stream));
+        RT_TRY(prepare<S>(gs[i], P[i], stream, &queue));
         active += P[i].active;
+        slice_bytes += P[i].slice_bytes;
     }
+    RT_TRY(flush_slices<S>(queue, stream));
+    prof_end(PROF_OZ_SLICE, stream, slice_bytes);
     for (int i = 0; i < n; ++i) RT_TRY(plan<S>(P[i], active, stream));
     for (int mode = 0; mode < 2; ++mode) {
         std::vector<Prepared*> grp;
