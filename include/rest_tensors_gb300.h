@@ -128,8 +128,9 @@ rt_status rt_dgemm_split(char opa, char opb, int m, int n, int k, const double* 
 /* special_dgemm_f_01_ on device memory and a stream: the same operation on
  * ten3_a[x_a, y_a, z_a] and matr_b[rows_b, columns_b], in place.  form
  * RT_FORM_FP64, or RT_FORM_SPLIT (nslices 3..8), whose product runs on the
- * tensor cores and then applies alpha and beta in float64.  Scratch: at most
- * 8 GB of staged y-slices (plus the split form's digit planes). */
+ * tensor cores and then applies alpha and beta in float64; its inputs must be
+ * finite (rt_sync_status then reports RT_ERR_NONFINITE otherwise).  Scratch:
+ * at most 8 GB of staged y-slices (plus the split form's digit planes). */
 rt_status rt_special_dgemm_01(double* ten3_a, int x_a, int y_a, int z_a, int start_x_a, int len_x_a, int start_z_a,
                               int len_z_a, const double* matr_b, int rows_b, int columns_b, int start_row_b,
                               int len_row_b, int start_column_b, int len_column_b, double alpha, double beta,

@@ -32,12 +32,14 @@ def declared_functions():
             m = re.match(r"^(?:extern \"C\" )?[A-Za-z_][\w\s\*]*?\b([A-Za-z_]\w*)\s*\(.*\)$", stmt)
             if m and not re.search(r"\b(static|inline|RT_SYNTH_FN)\b", stmt):
                 names.add(m.group(1))
-    return sorted(n for n in names if n.startswith(("rt_", "ri_", "general_")))
+    return sorted(n for n in names if n.startswith(("rt_", "ri_", "general_", "special_")))
 
 
 def test_header_declares_the_seam():
     names = declared_functions()
-    for n in ["ri_ao2mo_f_", "general_dgemm_f_", "rt_ri_ov_k", "rt_ri_ao2mo", "rt_ri_j", "rt_dgemm"]:
+    for n in ["ri_ao2mo_f_", "general_dgemm_f_", "special_dgemm_f_01_", "rt_ri_ov_k", "rt_ri_ao2mo", "rt_ri_j",
+              "rt_dgemm", "rt_special_dgemm_01", "rt_copy_rr", "rt_ri_transpose", "rt_ri_pack_symm",
+              "rt_newton_schulz_inv_sqrt"]:
         assert n in names
 
 
@@ -88,3 +90,47 @@ def test_dgemm_shape_check_mirrors_reference():
     with pytest.raises(ValueError):
         rt._dgemm(A, (range(0, 2), range(0, 3)), "N", A, (range(0, 2), range(0, 2)), "N",
                   A, (range(0, 2), range(0, 2)), 1.0, 0.0)
+
+
+# ----------------------------------------------- next rows: argument checks --
+def test_special_dgemm_rejects_blocks_before_touching_the_device():
+    L = rt.lib()
+    L.rt_special_dgemm_01.restype = ctypes.c_int
+    # matr_b block 7 x 6 with len_z_a 7
+    st = L.rt_special_dgemm_01(None, 7, 5, 12, 2, 4, 3, 7, None, 11, 13, 1, 7, 4, 6, ctypes.c_double(1.0),
+                               ctypes.c_double(0.0), 0, 7, None)
+    assert st == 1 and b"len_z_a" in L.rt_last_error()
+    # block of ten3_a outside the tensor
+    st = L.rt_special_dgemm_01(None, 7, 5, 12, 2, 6, 3, 7, None, 11, 13, 1, 7, 4, 7, ctypes.c_double(1.0),
+                               ctypes.c_double(0.0), 0, 7, None)
+    assert st == 1 and b"outside" in L.rt_last_error()
+    # split form with a bad slice count
+    st = L.rt_special_dgemm_01(None, 7, 5, 12, 2, 4, 3, 7, None, 11, 13, 1, 7, 4, 7, ctypes.c_double(1.0),
+                               ctypes.c_double(0.0), 1, 2, None)
+    assert st == 1
+
+
+def test_layout_calls_reject_bad_modes_orders_and_ranges():
+    L = rt.lib()
+    assert L.rt_copy_mr(2, 2, None, 6, 5, 0, 0, None, 4, 5, 6, 0, 0, 0, 3, None) == 1  # mode 3
+    assert b"mode" in L.rt_last_error()
+    assert L.rt_copy_rm(4, 2, None, 4, 5, 6, 1, 0, 0, 0, None, 6, 5, 0, 0, None) == 1  # rows 1..5 of 4
+    assert L.rt_copy_mm(3, 3, None, 2, 5, 0, 0, None, 4, 4, 0, 0, None) == 1  # source rows 0..3 of 2
+    assert L.rt_copy_rr(2, 2, 2, None, 2, 2, 2, 1, 0, 0, None, 4, 4, 4, 0, 0, 0, None) == 1
+    for bad in (b"iik", b"ij", b"xyz"):
+        assert L.rt_ri_transpose(None, 2, 3, 4, bad, None, None) == 1
+    assert L.rt_ri_pack_symm(None, -1, 3, None, None) == 1
+    # empty blocks are accepted and do nothing
+    assert L.rt_copy_mr(0, 2, None, 6, 5, 0, 0, None, 4, 5, 6, 0, 0, 0, 0, None) == 0
+    assert L.rt_ri_transpose(None, 0, 3, 4, b"kji", None, None) == 0
+
+
+def test_newton_schulz_rejects_bad_arguments():
+    L = rt.lib()
+    shifts = (ctypes.c_double * 1)(0.0)
+    call = lambda n, nshift, form, nsl: L.rt_newton_schulz_inv_sqrt(  # noqa: E731
+        None, n, ctypes.c_double(1e-8), ctypes.c_double(1.0), 10, shifts, nshift, form, nsl, None, None, None, None)
+    assert call(4, 0, 0, 7) == 1  # no level shift
+    assert call(0, 1, 0, 7) == 1  # empty matrix
+    assert call(4, 1, 1, 9) == 1  # split form, bad slice count
+    assert call(4, 1, 0, 7) == 1  # null pointers
