@@ -177,7 +177,7 @@ def test_empty_and_degenerate_shapes():
 
 
 # ------------------------------------------------------------ J and E_x --
-@pytest.mark.parametrize("nb,naux", [(20, 12), (33, 7), (100, 400)])
+@pytest.mark.parametrize("nb,naux", [(20, 12), (33, 7), (100, 400), (40, 1100)])
 def test_ri_j_matches_oracle(nb, naux):
     C, B = inputs(nb, naux, seed=1)
     D = np.asfortranarray(C[:, :5] @ C[:, :5].T)
