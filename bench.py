@@ -757,7 +757,7 @@ def main():
         e2e_full = {"value": replicas.job_throughput([FLOPS] * world, full_s) / 1e12, "unit": "TFLOP/s",
                     "ms_per_step": full_s * 1e3, "h2d_bytes_per_step": 8 * (NB * NB * NAUX + NB * NB),
                     "d2h_bytes_per_step": d2h,
-                    "path": "rt_ri_ov_k_host (C ABI, pinned host buffers, whole ri3ao copied)"}
+                    "path": "rt_ri_ov_k_host (C ABI, pinned host buffers, whole ri3ao read by the SMs over the host link)"}
         del hB
 
     outputs = None

@@ -324,7 +324,8 @@ rt_status rt_synth_coef_seed(uint64_t seed, int nb, double* M, void* stream);
 
 /* Host-pointer form of rt_ri_ov_k: copies C and B to the device, runs the
  * path, copies ov and K back, all on the given stream (synchronised on
- * return).  Host buffers may be pageable or pinned. */
+ * return).  Host buffers may be pageable or pinned; pinned ri3ao slabs are
+ * read by the SMs directly, pageable ones go through the copy engine. */
 rt_status rt_ri_ov_k_host(const double* C, const double* B, int nb, int naux, int nocc, int nvir, double* ov,
                           double* K, int form, int nslices, void* stream);
 
