@@ -258,6 +258,7 @@ __global__ void __launch_bounds__(256) slice_strided_kernel(SliceArgs a) {
 // operand instead of two); rows beyond the operand (tile padding) get zero digits.
 constexpr int kFusedRows = 16;    // contiguous-row slicer
 constexpr int kStridedRows = 16;  // strided-row slicer (8 rows at 3 CTAs/SM measured slower)
+constexpr int kStridedRowsWide = 8;  // 640 < K <= 1280: 8 rows, 32 k-groups of 8 per row
 template <int S, int NBLK, int RR>
 __device__ __forceinline__ void slice_strided_rowmax_body(const SliceArgs& a, int* __restrict__ emax_out,
                                                           int64_t blk) {
@@ -311,7 +312,7 @@ __device__ __forceinline__ void slice_strided_rowmax_body(const SliceArgs& a, in
 }
 
 template <int S, int NBLK, int RR>
-__global__ void __launch_bounds__(256, RR >= 16 ? 2 : 3)
+__global__ void __launch_bounds__(256, (RR >= 16 || NBLK > 3) ? 2 : 3)
     slice_strided_rowmax_kernel(SliceArgs a, int* __restrict__ emax_out) {
     slice_strided_rowmax_body<S, NBLK, RR>(a, emax_out, blockIdx.x);
 }
@@ -1034,6 +1035,17 @@ rt_status slice_operand(const Operand& op, int64_t K, int T, Sliced& out, cudaSt
             case 4: slice_strided_rowmax_kernel<S, 4, RR><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
             default: slice_strided_rowmax_kernel<S, (640 + 8 * KQN - 1) / (8 * KQN), RR>
                          <<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
+        }
+        RT_TRY(check_launch("slice_strided_rowmax_kernel"));
+    } else if (op.s0 == 1 && out.Kb * KB <= 1280) {
+        // Still one pass: 8 rows per CTA give each row 32 threads, so five
+        // register blocks of 8 k cover 1280 terms.
+        constexpr int RR = kStridedRowsWide, KQN = 256 / RR;
+        const unsigned grid = (unsigned)(out.tiles * T / RR);
+        switch ((int)ceil_div(out.Kb * KB, 8 * KQN)) {
+            case 3: slice_strided_rowmax_kernel<S, 3, RR><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
+            case 4: slice_strided_rowmax_kernel<S, 4, RR><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
+            default: slice_strided_rowmax_kernel<S, 5, RR><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
         }
         RT_TRY(check_launch("slice_strided_rowmax_kernel"));
     } else if (op.s0 == 1) {
