@@ -67,6 +67,50 @@ rt_status ri_ao2mo_split(const double* C, const double* B, double* R, int nb, in
 // chunks_per_item for "the whole contraction range in one work item".
 constexpr int kWholeRange = 1 << 30;
 
+// The three split-form products of the ov + RI-K path.
+// X^P = B^P C_occ:  A(m=(mu,P), k=nu) = B[mu + nb nu + nb^2 P], B(n=i, k=nu) = C[nu + nb i].
+// No split-K for the two transform products: a CTA's int64 range guard
+// depends on the terms it sums, so results then do not depend on how the
+// slabs are blocked (the host entry streams them in blocks of any size).
+OzGemm x_product(const double* C, const double* B, int nb, int64_t np, int nocc, double* X, int S) {
+    const int64_t per = (int64_t)nb * nocc;
+    OzGemm g;
+    g.K = nb;
+    g.A.p = B; g.A.rows = (int64_t)nb * np; g.A.div = nb;
+    g.A.s0 = 1; g.A.s1 = (int64_t)nb * nb; g.A.sk = nb;
+    g.B.p = C; g.B.rows = nocc; g.B.s0 = nb; g.B.sk = 1;
+    g.C.p = X; g.C.md = nb; g.C.ms0 = 1; g.C.ms1 = per; g.C.ns0 = nb;
+    g.nslices = S;
+    g.chunks_per_item = kWholeRange;
+    return g;
+}
+
+// ov^P = X^P^T C_vir:  A(m=(i,P), k=mu) = X[mu + nb m], B(n=a, k=mu) = C_vir[mu + nb a].
+OzGemm ov_product(const double* C, int nb, int64_t np, int nocc, int nvir, const double* X, double* ov, int S) {
+    const int64_t per = (int64_t)nb * nocc;
+    OzGemm g;
+    g.K = nb;
+    g.A.p = X; g.A.rows = (int64_t)nocc * np; g.A.s0 = nb; g.A.sk = 1;
+    g.B.p = C + per; g.B.rows = nvir; g.B.s0 = nb; g.B.sk = 1;
+    g.C.p = ov; g.C.md = nocc; g.C.ms0 = 1; g.C.ms1 = (int64_t)nocc * nvir; g.C.ns0 = nocc;
+    g.nslices = S;
+    g.chunks_per_item = kWholeRange;
+    return g;
+}
+
+// K = X X^T over k = (i, P):  A(m=mu, k) = X[mu + nb k], symmetric, B = A.
+OzGemm k_product(const double* X, int nb, int nocc, int naux, double* K, int S) {
+    OzGemm g;
+    g.K = (int64_t)nocc * naux;
+    g.A.p = X; g.A.rows = nb; g.A.s0 = 1; g.A.sk = nb;
+    g.B = g.A;
+    g.b_is_a = true;
+    g.symmetric = true;
+    g.C.p = K; g.C.ms0 = 1; g.C.ns0 = nb;
+    g.nslices = S;
+    return g;
+}
+
 rt_status ri_ov_block(const double* C, const double* B, int nb, int64_t np, int nocc, int nvir, double* X,
                       double* ov, int form, int S, cudaStream_t stream) {
     const int64_t per = (int64_t)nb * nocc;
@@ -87,30 +131,8 @@ rt_status ri_ov_block(const double* C, const double* B, int nb, int64_t np, int 
         }
         return RT_OK;
     }
-    // A(m=(mu,P), k=nu) = B[mu + nb nu + nb^2 P], B(n=i, k=nu) = C[nu + nb i]
-    OzGemm g1;
-    g1.K = nb;
-    g1.A.p = B; g1.A.rows = (int64_t)nb * np; g1.A.div = nb;
-    g1.A.s0 = 1; g1.A.s1 = (int64_t)nb * nb; g1.A.sk = nb;
-    g1.B.p = C; g1.B.rows = nocc; g1.B.s0 = nb; g1.B.sk = 1;
-    g1.C.p = X; g1.C.md = nb; g1.C.ms0 = 1; g1.C.ms1 = per; g1.C.ns0 = nb;
-    g1.nslices = S;
-    // No split-K for the two transform products: a CTA's int64 range guard
-    // depends on the terms it sums, so results then do not depend on how the
-    // slabs are blocked (the host entry streams them in blocks of any size).
-    g1.chunks_per_item = kWholeRange;
-    RT_TRY(oz_gemm(g1, stream));
-    if (ov && nvir > 0) {
-        // A(m=(i,P), k=mu) = X[mu + nb m], B(n=a, k=mu) = C_vir[mu + nb a]
-        OzGemm g2;
-        g2.K = nb;
-        g2.A.p = X; g2.A.rows = (int64_t)nocc * np; g2.A.s0 = nb; g2.A.sk = 1;
-        g2.B.p = C + per; g2.B.rows = nvir; g2.B.s0 = nb; g2.B.sk = 1;
-        g2.C.p = ov; g2.C.md = nocc; g2.C.ms0 = 1; g2.C.ms1 = (int64_t)nocc * nvir; g2.C.ns0 = nocc;
-        g2.nslices = S;
-        g2.chunks_per_item = kWholeRange;
-        RT_TRY(oz_gemm(g2, stream));
-    }
+    RT_TRY(oz_gemm(x_product(C, B, nb, np, nocc, X, S), stream));
+    if (ov && nvir > 0) RT_TRY(oz_gemm(ov_product(C, nb, np, nocc, nvir, X, ov, S), stream));
     return RT_OK;
 }
 
@@ -127,15 +149,7 @@ rt_status ri_k_from_x(const double* X, int nb, int nocc, int naux, double* K, in
         g3.splitk = (int)std::max<int64_t>(1, std::min<int64_t>(want, kdim / 256));
         return gemm_f64(g3, stream);
     }
-    OzGemm g3;
-    g3.K = kdim;
-    g3.A.p = X; g3.A.rows = nb; g3.A.s0 = 1; g3.A.sk = nb;
-    g3.B = g3.A;
-    g3.b_is_a = true;
-    g3.symmetric = true;
-    g3.C.p = K; g3.C.ms0 = 1; g3.C.ns0 = nb;
-    g3.nslices = S;
-    return oz_gemm(g3, stream);
+    return oz_gemm(k_product(X, nb, nocc, naux, K, S), stream);
 }
 
 rt_status ri_ov_k_split(const double* C, const double* B, int nb, int naux, int nocc, int nvir, double* ov,

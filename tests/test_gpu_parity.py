@@ -325,3 +325,25 @@ def test_symmetric_host_entry_mirrors_the_upper_triangle(nb):
     if nvir:
         assert relerr(hO[:nocc * nvir * naux].reshape(nocc, nvir, naux, order="F"), ov_ref) < 1e-12
     assert relerr(hK.reshape(nb, nb, order="F"), K_ref) < 1e-12
+
+
+def test_split_ov_k_replays_from_a_cuda_graph():
+    """The single-molecule split path captured in a CUDA graph (scratch as graph
+    allocation nodes) replays to the uncaptured result, bit for bit."""
+    nb, naux, nocc = 64, 48, 8
+    C, B = inputs(nb, naux, seed=3)
+    dC, dB = dev(C), dev(B)
+    ov0, K0 = rt.ri_ov_k(dC, dB, nb, naux, nocc, nb - nocc, form="split")  # uncaptured first call
+    torch.cuda.synchronize()
+    ov = torch.zeros_like(ov0)
+    K = torch.zeros_like(K0)
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        rt.ri_ov_k(dC, dB, nb, naux, nocc, nb - nocc, ov=ov, K=K, form="split", stream=s)
+    for _ in range(2):
+        g.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(ov, ov0) and torch.equal(K, K0)
+    _, K_ref = oracle.ri_ov_k(C, B, nocc)
+    assert relerr(host(K, (nb, nb)), K_ref) < 1e-11
