@@ -105,10 +105,18 @@ __global__ void multi_axpy_kernel(double* __restrict__ X, int64_t ld, int nv, co
     }
 }
 
-// y = x / s  (host scalar; division as in the reference's `x /= norm`)
-__global__ void div_kernel(double* __restrict__ y, const double* __restrict__ x, double s, int64_t n) {
+// y = x / s  (host scalar; division as in the reference's `x /= norm`; y may equal x)
+__global__ void div_kernel(double* y, const double* x, double s, int64_t n) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         y[i] = x[i] / s;
+}
+
+// y = x / sqrt(*d2)  (a norm kept on the device; sqrt is correctly rounded, as on the host)
+// (called in place: y may equal x)
+__global__ void div_dev_sqrt_kernel(double* y, const double* x, const double* __restrict__ d2, int64_t n) {
+    const double v = sqrt(*d2);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = x[i] / v;
 }
 
 // r = ax - e * x
@@ -449,10 +457,35 @@ rt_status rt_davidson_solve(rt_matvec_fn a_x, void* ctx, const double* x0_1d, co
     ScratchBuf vb;
     RT_TRY(scratch_alloc(vb, sizeof(double) * (size_t)cap * cap, s));
     double* Vdev = vb.as<double>();
-    // dst[n, cols] = src[n, rows] * V[rows, cols] with V on the host (_gen_x0, davidson.rs:392-404).
-    auto gen_x0 = [&](const double* src, const double* V, int rows, int cols, double* dst) -> rt_status {
+    // The Ritz coefficients go up through page-locked staging, so the upload does
+    // not wait for the stream; `vdone` marks when the staging may be rewritten.
+    double* Vpin = nullptr;
+    RT_CUDA_TRY(cudaMallocHost(&Vpin, sizeof(double) * (size_t)cap * cap));
+    cudaEvent_t vdone = nullptr;
+    if (cudaEventCreateWithFlags(&vdone, cudaEventDisableTiming) != cudaSuccess) {
+        cudaFreeHost(Vpin);
+        RT_CUDA_TRY(cudaGetLastError());
+    }
+    struct Staging {
+        double* p;
+        cudaEvent_t e;
+        ~Staging() {
+            if (e) cudaEventSynchronize(e);
+            if (e) cudaEventDestroy(e);
+            if (p) cudaFreeHost(p);
+        }
+    } staging{Vpin, vdone};
+    auto upload_v = [&](const double* V, int rows, int cols) -> rt_status {
+        if ((int64_t)rows * cols == 0) return RT_OK;
+        RT_CUDA_TRY(cudaEventSynchronize(vdone));
+        std::copy(V, V + (size_t)rows * cols, Vpin);
+        RT_CUDA_TRY(cudaMemcpyAsync(Vdev, Vpin, sizeof(double) * (size_t)rows * cols, cudaMemcpyHostToDevice, s));
+        RT_CUDA_TRY(cudaEventRecord(vdone, s));
+        return RT_OK;
+    };
+    // dst[n, cols] = src[n, rows] * V[rows, cols] with V uploaded (_gen_x0, davidson.rs:392-404).
+    auto gen_x0 = [&](const double* src, int rows, int cols, double* dst) -> rt_status {
         if (cols == 0) return RT_OK;
-        RT_CUDA_TRY(cudaMemcpyAsync(Vdev, V, sizeof(double) * (size_t)rows * cols, cudaMemcpyHostToDevice, s));
         RT_TRY(rt_dgemm('N', 'N', (int)n, cols, rows, 1.0, src, (int)n, Vdev, rows, 0.0, dst, (int)n, s));
         return RT_OK;
     };
@@ -469,7 +502,33 @@ rt_status rt_davidson_solve(rt_matvec_fn a_x, void* ctx, const double* x0_1d, co
     auto col = [&](double* base, int j) { return base + (size_t)j * n; };
 
     // Modified Gram-Schmidt of the columns of src (count m) into dst; returns the kept count.
+    // First an optimistic pass that keeps every vector: each norm stays on the device
+    // and the norms are read back once.  If all pass the reference's test, the result
+    // is the one the vector-by-vector pass below gives (same dot kernel, same
+    // correctly rounded sqrt); otherwise that pass runs again from src.
     auto qr = [&](double* dst, const double* src, int m, int* kept) -> rt_status {
+        if (m > 0 && m <= ops.ncolout) {
+            for (int i = 0; i < m; ++i) {
+                double* xi = col(dst, i);
+                if (xi != src + (size_t)i * n) RT_TRY(ops.copy(xi, src + (size_t)i * n, n));
+                for (int j = 0; j < i; ++j) RT_TRY(ops.project_out(xi, col(dst, j), n));
+                RT_TRY(ops.dot(xi, xi, n, ops.colout + i));
+                div_dev_sqrt_kernel<<<ops.grid, 256, 0, s>>>(xi, xi, ops.colout + i, n);
+                RT_TRY(check_launch("div_dev_sqrt_kernel"));
+            }
+            std::vector<double> d2(m);
+            RT_CUDA_TRY(cudaMemcpyAsync(d2.data(), ops.colout, sizeof(double) * m, cudaMemcpyDeviceToHost, s));
+            RT_CUDA_TRY(cudaStreamSynchronize(s));
+            bool all = true;
+            for (int i = 0; i < m; ++i) {
+                const double norm = sqrt(d2[i]);
+                all = all && norm * norm > lindep;
+            }
+            if (all) {
+                *kept = m;
+                return RT_OK;
+            }
+        }
         int nv = 0;
         for (int i = 0; i < m; ++i) {
             double* xi = col(dst, nv);
@@ -571,8 +630,9 @@ rt_status rt_davidson_solve(rt_matvec_fn a_x, void* ctx, const double* x0_1d, co
         ev.assign(w.begin(), w.begin() + nroots_current);
         vmat.assign(z.begin(), z.begin() + (size_t)space * nroots_current);
         // x0 = XS v, ax0 = AX v  (_gen_x0, davidson.rs:392-404)
-        RT_TRY(gen_x0(XS, vmat.data(), space, nroots_current, X0));
-        RT_TRY(gen_x0(AXs, vmat.data(), space, nroots_current, AX0));
+        RT_TRY(upload_v(vmat.data(), space, nroots_current));
+        RT_TRY(gen_x0(XS, space, nroots_current, X0));
+        RT_TRY(gen_x0(AXs, space, nroots_current, AX0));
         dxn.assign(nroots_current, 0.0);
         de.assign(nroots_current, 0.0);
         bool all_conv = true;
@@ -592,7 +652,8 @@ rt_status rt_davidson_solve(rt_matvec_fn a_x, void* ctx, const double* x0_1d, co
         if (max_dx > 1.0 && max_dx / max_dx_last > 3.0 && space > nroots + 2) {
             // Restore the previous Ritz vectors and restart (davidson.rs:210-217).
             const int nl = (int)(vlast.size() / std::max(head, 1));
-            RT_TRY(gen_x0(XS, vlast.data(), head, nl, XT));
+            RT_TRY(upload_v(vlast.data(), head, nl));
+            RT_TRY(gen_x0(XS, head, nl, XT));
             x0src = XT;
             nx0 = nl;
             fresh = true;
