@@ -55,3 +55,15 @@ def test_failed_stage_retries_six_times_with_halved_mixing():
 def test_empty_level_shift_is_rejected():
     with pytest.raises(ValueError):
         oracle.newton_schulz_inverse_square_root_v02(spd(3), 1e-8, 1.0, 10, [])
+
+
+def test_reference_sqrt_inverse_matrix_is_out_of_reach_of_the_iteration():
+    # The SPD matrix of the reference's test_sqrt_inverse (matrix_blas_lapack.rs:1398-1405), which the
+    # reference inverts with lapack_power.  Its condition number is ~6600; the uncoupled iteration
+    # X <- 0.5 X (3I - A X X) reaches ||dX|| / n^2 ~ 3e-5 and then amplifies rounding, so the reference's
+    # algorithm never converges: the stage and its six halved-mixing retries each run all 101 evaluations.
+    A = np.array([[4.0, 12.0, -16.0], [12.0, 37.0, -43.0], [-16.0, -43.0, 98.0]])
+    assert np.linalg.cond(A) > 6000
+    _, _, conv, evals = oracle.newton_schulz_inverse_square_root_v02(A, 1e-10, 1.0, 100, [0.0])
+    assert not conv
+    assert evals == 7 * 101
