@@ -64,6 +64,9 @@ def parse():
     p.add_argument("--outputs", type=int, default=1,
                    help="also time the full ri3mo transform and the (ia|jb) block of this workload (0: skip)")
     p.add_argument("--large-steps", type=int, default=3)
+    p.add_argument("--dropin", type=int, default=1,
+                   help="also time the drop-in ri_ao2mo_f_ end to end on host buffers, both forms (0: skip)")
+    p.add_argument("--dropin-child", action="store_true", help=argparse.SUPPRESS)
     p.add_argument("--ri3fn", type=int, default=1,
                    help="also time the ri3fn metric step (special_dgemm_f_01) on this workload's tensor (0: skip)")
     return p.parse_args()
@@ -186,6 +189,26 @@ def batched_leg(args, rt, torch, stream):
     out.update(res)
     out["speedup_vs_fp64"] = res["fp64"]["ms_per_step"] / res["split"]["ms_per_step"]
     out["errors_vs_fp64"] = {"ov_max_abs": ov_err, "K_max_rel": k_err}
+    if not args.no_cpu:
+        # The oracle on every molecule's own inputs (copied back from the device), as checker of both forms.
+        import numpy as np
+
+        import oracle
+
+        oracle.set_threads(os.cpu_count() or 1)
+        ev = {f: {"ov_max_abs": 0.0, "K_max_rel": 0.0} for f in ("fp64", "split")}
+        t0 = time.perf_counter()
+        for q, r in zip(probs, ref):
+            nb, naux, nocc, nvir = q["nb"], q["naux"], q["nocc"], q["nvir"]
+            ov_o, K_o = oracle.ri_ov_k(fortran_view(q["C"], (nb, nb)), fortran_view(q["B"], (nb, nb, naux)), nocc)
+            for f, (ovd, Kd) in (("fp64", r), ("split", (q["ov"], q["K"]))):
+                ev[f]["ov_max_abs"] = max(ev[f]["ov_max_abs"],
+                                          float(np.abs(fortran_view(ovd, (nocc, nvir, naux)) - ov_o).max()))
+                ev[f]["K_max_rel"] = max(ev[f]["K_max_rel"], float(np.abs(fortran_view(Kd, (nb, nb)) - K_o).max()
+                                                                   / np.abs(K_o).max()))
+        ev["inputs"] = f"all {len(probs)} molecules, the device's inputs copied to the host"
+        ev["oracle_seconds"] = time.perf_counter() - t0
+        out["errors_vs_oracle"] = ev
     del probs, ref
     torch.cuda.empty_cache()
     return out
@@ -233,6 +256,33 @@ def large_leg(args, rt, torch, stream):
     out["errors_vs_fp64"] = {"ov_max_abs": float((ov - ov64).abs().max()),
                              "K_max_rel": float((K - K64).abs().max() / K64.abs().max()),
                              "ex_abs": abs(ex - ex64), "ex_fp64": ex64}
+    if not args.no_cpu:
+        # The oracle on a slab subset (the whole tensor is 55 GB): the measured run's ov slabs
+        # against it in both forms, and K and E_x over the same slabs from the GPU entry point.
+        import numpy as np
+
+        import oracle
+
+        oracle.set_threads(os.cpu_count() or 1)
+        nsub = 96
+        Bs = B[: nsub * nb * nb]
+        t0 = time.perf_counter()
+        Ch = fortran_view(C, (nb, nb))
+        ov_o, K_o = oracle.ri_ov_k(Ch, fortran_view(Bs, (nb, nb, nsub)), nocc)
+        Co = Ch[:, :nocc]
+        ex_o = oracle.exchange_energy(np.asfortranarray(Co @ Co.T), K_o)
+        ev = {"inputs": f"slabs 0..{nsub - 1} of {naux}, the device's inputs copied to the host",
+              "oracle_seconds": time.perf_counter() - t0, "ex_oracle_subset": ex_o}
+        nsl = nocc * nvir * nsub
+        for f, ovd in (("fp64", ov64), ("split", ov)):
+            _, Ks = rt.ri_ov_k(C, Bs, nb, nsub, nocc, nvir, form=f, nslices=S, want_ov=False, stream=stream)
+            ex_s = rt.exchange_energy(D, Ks, nb).item()
+            ev[f] = {"ov_max_abs": float(np.abs(fortran_view(ovd[:nsl], (nocc, nvir, nsub)) - ov_o).max()),
+                     "K_max_rel": float(np.abs(fortran_view(Ks, (nb, nb)) - K_o).max() / np.abs(K_o).max()),
+                     "ex_abs": abs(ex_s - ex_o)}
+            del Ks
+        out["errors_vs_oracle"] = ev
+        del Bs
     J = rt.ri_j(B, D, nb, naux)[1]
     out["J_norm"] = float(J.norm())
     del ov64, K64, J
@@ -327,6 +377,74 @@ def outputs_leg(args, rt, torch, stream, B, C, ov):
                    "max_rel_err": float((msp - m64).abs().max() / m64.abs().max())}
     del m64, msp
     torch.cuda.empty_cache()
+    return res
+
+
+# ------------------------------------------ the drop-in ri_ao2mo_f_ end to end --
+def dropin_ao2mo_once(rt, Ch, Bh, R):
+    """One warm-up call and one timed call of the ri_ao2mo_f_ symbol on pageable host buffers."""
+    rt.ri_ao2mo_f(Ch, Bh, R, NB, NB, NAUX)
+    t0 = time.perf_counter()
+    rt.ri_ao2mo_f(Ch, Bh, R, NB, NB, NAUX)
+    return time.perf_counter() - t0
+
+
+def dropin_child(args):
+    """Child process of the drop-in leg (run with RT_FORM set): the same inputs, the symbol timed once
+    after a warm-up, the result compared with the device float64 transform."""
+    import numpy as np
+    import torch
+
+    import rest_tensors_gb300 as rt
+
+    B = rt.synth_ri3ao(args.seed, NB, NAUX)
+    C = rt.synth_coef(args.seed, NB)
+    Bh, Ch = B.cpu().numpy(), C.cpu().numpy()
+    R = np.empty(NAUX * NB * NB)
+    dt = dropin_ao2mo_once(rt, Ch, Bh, R)
+    R64 = rt.ri_ao2mo(C, B, NB, NB, NAUX, form="fp64").cpu().numpy()
+    torch.cuda.synchronize()
+    print(json.dumps({"seconds": dt, "max_abs_vs_device_fp64": float(np.abs(R - R64).max())}), flush=True)
+
+
+def dropin_ao2mo_leg(args, rt, B, C):
+    """ri_ao2mo_f_ (the reference's own seam, src/external_libs/ffi_restmatr.rs:5-11) end to end on pageable
+    host buffers, as a Rust Vec would be: the full transform [naux, nbas, nbas] (2.07e12 FLOP), with 6.9 GB in
+    and 6.9 GB out inside the timing.  Float64 (the default) in this process; the split form in a child
+    process with RT_FORM=split, because the seam reads its form once per process."""
+    import numpy as np
+
+    fl = NAUX * 4.0 * NB ** 3
+    Bh, Ch = B.cpu().numpy(), C.cpu().numpy()
+    R = np.empty(NAUX * NB * NB)
+    res = {"flop": fl, "h2d_bytes": 8 * (NB * NB * NAUX + NB * NB), "d2h_bytes": 8 * NAUX * NB * NB,
+           "host_memory": "pageable (numpy), as a Rust Vec", "path": "ri_ao2mo_f_ -> rt_ri_ao2mo_host"}
+    if os.environ.get("RT_FORM", "fp64").lower() in ("", "fp64"):
+        dt = dropin_ao2mo_once(rt, Ch, Bh, R)
+        res["fp64"] = {"ms": dt * 1e3, "tflops": fl / dt / 1e12}
+    del R
+    env = {**os.environ, "RT_FORM": "split", "RT_NSLICES": str(args.nslices)}
+    r = subprocess.run([sys.executable, os.path.abspath(__file__), "--dropin-child", "--seed", str(args.seed)],
+                       env=env, capture_output=True, text=True, timeout=900)
+    if r.returncode == 0 and r.stdout.strip():
+        d = json.loads(r.stdout.strip().splitlines()[-1])
+        res["split"] = {"ms": d["seconds"] * 1e3, "tflops": fl / d["seconds"] / 1e12, "nslices": args.nslices,
+                        "max_abs_vs_device_fp64": d["max_abs_vs_device_fp64"], "env": "RT_FORM=split"}
+    else:
+        res["split"] = {"error": (r.stderr or r.stdout)[-400:]}
+    if not args.no_cpu:
+        import oracle
+
+        oracle.set_threads(os.cpu_count() or 1)
+        nsl = 240
+        Bf = Bh.reshape(NAUX, NB, NB).transpose(2, 1, 0)
+        Cf = Ch.reshape(NB, NB).T
+        oracle.ri_ao2mo(Cf, Bf[:, :, :24])  # warm-up
+        t0 = time.perf_counter()
+        oracle.ri_ao2mo(Cf, Bf[:, :, :nsl])
+        dt = time.perf_counter() - t0
+        res["cpu"] = {"tflops": nsl * 4.0 * NB ** 3 / dt / 1e12, "cores": oracle.get_threads(), "seconds": dt,
+                      "sample": f"{nsl} of {NAUX} aux slabs, C restatement of restmatr.f90:158-194 over OpenBLAS"}
     return res
 
 
@@ -518,33 +636,55 @@ def layout_leg(args, rt, torch, stream, B):
 
 
 # ------------------------------------------------------------ CPU baseline --
-def cpu_baseline(seed: int, budget_s: float = 12.0):
-    """Oracle (C restatement of restmatr.f90 + OpenBLAS, all host threads) on a bounded slab range."""
+def fortran_view(t, shape):
+    """Host numpy view of a flat column-major device tensor, Fortran-ordered (no copy after the transfer)."""
+    return t.cpu().numpy().reshape(tuple(reversed(shape))).transpose(*reversed(range(len(shape))))
+
+
+def cpu_baseline(B, C, outs, budget_s: float = 12.0):
+    """The oracle (C restatement of restmatr.f90 + OpenBLAS, all host threads) on the same inputs the
+    GPU ran, copied back from the device: timed over a bounded slab range (the whole workload when it
+    fits the budget) as the CPU baseline, and run over every slab as the checker of the GPU outputs.
+
+    outs: {form: (ov, K, E_x)} device results of the measured workload."""
     import numpy as np
 
     import oracle
 
     cores = os.cpu_count() or 1
     oracle.set_threads(cores)
-    C = oracle.synth_coef(seed, NB)
+    Bh = fortran_view(B, (NB, NB, NAUX))
+    Ch = fortran_view(C, (NB, NB))
     probe = 24
-    B = oracle.synth_ri3ao(seed, NB, NAUX, 0, probe)
-    oracle.ri_ov_k(C, B, NOCC)  # warm-up (threads, pages)
+    oracle.ri_ov_k(Ch, Bh[:, :, :probe], NOCC)  # warm-up (threads, pages)
     t0 = time.perf_counter()
-    oracle.ri_ov_k(C, B, NOCC)
+    oracle.ri_ov_k(Ch, Bh[:, :, :probe], NOCC)
     per_slab = (time.perf_counter() - t0) / probe
     nslab = int(max(probe, min(NAUX, budget_s / max(per_slab, 1e-9))))
-    B = oracle.synth_ri3ao(seed, NB, NAUX, 0, nslab)
     t0 = time.perf_counter()
-    oracle.ri_ov_k(C, B, NOCC)
+    ov_ref, K_ref = oracle.ri_ov_k(Ch, Bh[:, :, :nslab], NOCC)
     dt = time.perf_counter() - t0
-    del B
-    np.asarray(0)
-    return {"value": nslab * FLOPS_PER_SLAB / dt / 1e12, "unit": "TFLOP/s", "cores": oracle.get_threads(),
-            "kind": "port",
-            "sample": f"{nslab} of {NAUX} aux slabs of the same workload ({dt:.1f} s), C restatement of "
-                      f"restmatr.f90 per-slab dgemms over OpenBLAS (scipy bundle)",
-            "seconds": dt}
+    if nslab < NAUX:
+        ov_ref, K_ref = oracle.ri_ov_k(Ch, Bh, NOCC)
+    Co = Ch[:, :NOCC]
+    ex_ref = oracle.exchange_energy(np.asfortranarray(Co @ Co.T), K_ref)
+    errs = {}
+    for form, (ov, K, ex) in outs.items():
+        ov_h = fortran_view(ov, (NOCC, NVIR, NAUX))
+        K_h = fortran_view(K, (NB, NB))
+        errs[form] = {"ov_max_abs": float(np.abs(ov_h - ov_ref).max()),
+                      "ov_max_rel": float(np.abs(ov_h - ov_ref).max() / np.abs(ov_ref).max()),
+                      "K_max_rel": float(np.abs(K_h - K_ref).max() / np.abs(K_ref).max()),
+                      "ex_abs": abs(ex - ex_ref), "ex_rel": abs(ex - ex_ref) / abs(ex_ref)}
+    errs["ex_oracle"] = ex_ref
+    errs["inputs"] = "the device's ri3ao and C, copied to the host; oracle over all slabs"
+    del Bh, ov_ref, K_ref
+    cpu = {"value": nslab * FLOPS_PER_SLAB / dt / 1e12, "unit": "TFLOP/s", "cores": oracle.get_threads(),
+           "kind": "port",
+           "sample": f"{nslab} of {NAUX} aux slabs of the same workload ({dt:.2f} s), C restatement of "
+                     f"restmatr.f90 per-slab dgemms over OpenBLAS (scipy bundle)",
+           "seconds": dt}
+    return cpu, errs
 
 
 def run_reference(args, rank: int):
@@ -600,6 +740,9 @@ def main():
     if args.impl == "reference":
         run_reference(args, rank)
         return
+    if args.dropin_child:
+        dropin_child(args)
+        return
     assert args.warmup >= 3, "at least 3 warm-up steps"
     import torch
 
@@ -652,6 +795,15 @@ def main():
     ov64, K64 = ov.clone(), K.clone()
     ex64 = rt.exchange_energy(D, K64, NB).item()
     fp64_ms, _ = timed("fp64", 0, args.fp64_steps)
+    # The allocation-free float64 entry (fixed 32 MiB scratch, slabs streamed through it), one call.
+    rt.ri_ov_k_fp64_noalloc(C, B, NB, NAUX, NOCC, NVIR, ov=ov, K=K, stream=stream)
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    rt.ri_ov_k_fp64_noalloc(C, B, NB, NAUX, NOCC, NVIR, ov=ov, K=K, stream=stream)
+    e1.record(stream)
+    barrier()
+    noalloc_ms = e0.elapsed_time(e1)
     # Accurate E_x reference: the occupied-occupied block B_ij^P = (C_occ^T B^P C_occ)_ij
     # in float64 (600-term dot products per element), then -sum of squares with a tree sum.
     Coo = torch.cat([C[: NB * NOCC], C[: NB * NOCC]])
@@ -703,6 +855,13 @@ def main():
                 "launches_per_step": g_n / args.steps, "share_of_step": g_ms / (ms * args.steps),
                 "slicing": {"kernel": "emax/slice kernels (HBM)", "achieved_gbs": s_bytes / s_ms / 1e6 if s_ms else None,
                             "peak_gbs": pk.get("hbm_gbs"), "share_of_step": s_ms / (ms * args.steps)}}
+
+    # ---- CPU baseline, and the oracle as checker of both forms' outputs at this workload
+    cpu = errors_vs_oracle = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        ex_sp = rt.exchange_energy(D, K, NB).item()
+        cpu, errors_vs_oracle = cpu_baseline(B, C, {"fp64": (ov64, K64, ex64), "split": (ov, K, ex_sp)})
+    del ov64, K64
 
     # ---- RI-J: two streaming passes over ri3ao (HBM-bound), timed on its own
     w_j = torch.empty(NAUX, dtype=torch.float64, device=dev)
@@ -764,6 +923,10 @@ def main():
     if args.outputs:
         outputs = outputs_leg(args, rt, torch, stream, B, C, ov)
 
+    dropin = None
+    if args.dropin and world == 1:
+        dropin = dropin_ao2mo_leg(args, rt, B, C)
+
     ri3fn = None
     if args.ri3fn:
         ri3fn = ri3fn_leg(args, rt, torch, stream, B)
@@ -782,10 +945,6 @@ def main():
         torch.cuda.empty_cache()
         large = large_leg(args, rt, torch, stream)
 
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline(args.seed)
-
     if rank != 0:
         return
     line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
@@ -796,14 +955,18 @@ def main():
                        "nslices": S, "l2": "inputs larger than L2 (6.9 GB ri3ao read per step)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "fp64": {"value": world * FLOPS / fp64_ms / 1e9, "unit": "TFLOP/s", "ms_per_step": fp64_ms,
-                     "form": "float64 DFMA tiled GEMM"},
+                     "form": "float64 DFMA tiled GEMM",
+                     "noalloc": {"ms": noalloc_ms, "tflops": FLOPS / noalloc_ms / 1e9,
+                                 "entry": "rt_ri_ov_k_fp64_noalloc (no device allocation; 32 MiB fixed scratch)"}},
             "speedup_vs_fp64": fp64_ms / ms,
-            "errors_vs_fp64": err, "gpu_launches": launches, "clocks": clocks, "roofline": roofline,
+            "errors_vs_fp64": err, "errors_vs_oracle": errors_vs_oracle, "gpu_launches": launches, "clocks": clocks, "roofline": roofline,
             "e2e": e2e, "e2e_full_input": e2e_full, "rij": rij, "cpu_baseline": cpu}
     if sweep:
         line["sweep"] = sweep
     if outputs:
         line["outputs"] = outputs
+    if dropin:
+        line["e2e_dropin_ao2mo"] = dropin
     if ri3fn:
         line["ri3fn"] = ri3fn
     if batched:

@@ -65,12 +65,21 @@ rt_status rt_sync_status(void* stream);
 
 /* ------------------------------------------------------------------------
  * Drop-in Fortran seam (host pointers).
+ *
+ * Precision form of the three drop-ins: read once per process from the
+ * environment, RT_FORM = fp64 (default) or split, and RT_NSLICES = 3..8
+ * (digits per float64 in the split form, default 7).  Unchanged callers get the
+ * float64 form; a deployment opts in to the split form without relinking.
+ * An unrecognised value makes every drop-in call fail (rt_last_status() is
+ * RT_ERR_INVALID_ARG) instead of running another form.  No counterpart in the
+ * reference, whose seam is float64 only.
  * ------------------------------------------------------------------------ */
 
 /* Replaces ri_ao2mo_f_ (src/external_libs/ffi_restmatr.rs:5-11, implemented at
  * src/external_libs/restmatr.f90:158-194):
  *   ri3mo[P,p,q] = sum_{mu,nu} eigenvector[mu,p] ri3fn[mu,nu,P] eigenvector[nu,q]
- * ri3mo is [num_auxbas, num_states, num_states] (P fastest).  Float64 form.
+ * ri3mo is [num_auxbas, num_states, num_states] (P fastest).  Runs
+ * rt_ri_ao2mo_host in the seam's form on the per-thread default stream.
  * Failures are reported through rt_last_status()/rt_last_error() (the Fortran
  * subroutine has no return value) and ri3mo is then left zero-filled. */
 void ri_ao2mo_f_(const double* eigenvector, const double* ri3fn, double* ri3mo, const int* num_states,
@@ -79,7 +88,9 @@ void ri_ao2mo_f_(const double* eigenvector, const double* ri3fn, double* ri3mo, 
 /* Replaces general_dgemm_f_ (src/external_libs/ffi_restmatr.rs:13-24,
  * restmatr.f90:63-107): on column-major host matrices,
  *   C[rc, cc] = alpha * op_a(A[ra, ca]) * op_b(B[rb, cb]) + beta * C[rc, cc]
- * with blocks given by 0-based start and length. */
+ * with blocks given by 0-based start and length.  In the split form the
+ * product is formed from digit planes and alpha, beta are applied in float64
+ * (beta = 0 does not read C). */
 void general_dgemm_f_(const double* matr_a, const int* rows_a, const int* columns_a, const int* start_row_a,
                       const int* len_row_a, const int* start_column_a, const int* len_column_a, const char* opa,
                       const double* matr_b, const int* rows_b, const int* columns_b, const int* start_row_b,
@@ -98,8 +109,8 @@ void general_dgemm_f_(const double* matr_a, const int* rows_a, const int* column
  * i_y_a is accepted and ignored, as in the Fortran, which loops over all
  * y-slices.  The Fortran body hands one buffer to dgemm as both A and C; this
  * entry computes the product those arguments describe, from an unaliased
- * copy.  Float64 form.  Failures are reported through rt_last_status() /
- * rt_last_error() and leave ten3_a unchanged. */
+ * copy.  Runs in the seam's form.  Failures are reported through
+ * rt_last_status() / rt_last_error() and leave ten3_a unchanged. */
 void special_dgemm_f_01_(double* ten3_a, const int* x_a, const int* y_a, const int* z_a, const int* start_x_a,
                          const int* len_x_a, const int* i_y_a, const int* start_z_a, const int* len_z_a,
                          const double* matr_b, const int* rows_b, const int* columns_b, const int* start_row_b,
@@ -151,10 +162,10 @@ rt_status rt_ri_ov_k(const double* C, const double* B, int nb, int naux, int noc
                      int form, int nslices, void* stream);
 
 /* Allocation-free float64 form of rt_ri_ov_k, for callers that cannot
- * allocate device memory while they run (inside a stream capture that must
- * hold no allocation nodes, under a fixed external memory arena, or on a
- * serving path where cudaMalloc/cudaFree and their implicit synchronisation
- * are not allowed).  It has no counterpart in the reference.  The half-
+ * allocate device memory while they run: a host runtime that has handed the
+ * GPU's memory to a fixed arena it manages itself, or a serving path on which
+ * cudaMalloc/cudaFree, and the device synchronisation they imply, are not
+ * allowed.  It has no counterpart in the reference.  The half-
  * transform goes through one fixed 32 MiB device array that the library
  * holds on every GPU that loads it, so nb*nocc may be at most 4,194,304
  * (larger requests fail with RT_ERR_INVALID_ARG); the aux slabs stream through
@@ -328,6 +339,17 @@ rt_status rt_synth_coef_seed(uint64_t seed, int nb, double* M, void* stream);
  * read by the SMs directly, pageable ones go through the copy engine. */
 rt_status rt_ri_ov_k_host(const double* C, const double* B, int nb, int naux, int nocc, int nvir, double* ov,
                           double* K, int form, int nslices, void* stream);
+
+/* Host-pointer form of rt_ri_ao2mo (the full transform ri3mo[P,p,q], P
+ * fastest), pipelined over the host link: ri3ao slab blocks stream in while
+ * the half-transform of the previous block runs, and ri3mo is produced in
+ * blocks of q columns (contiguous in the P-fastest layout) whose copies back
+ * overlap the next block's GEMM.  Host buffers may be pageable (a Rust Vec) or
+ * pinned.  Every element equals rt_ri_ao2mo's on the same inputs.  Needs
+ * about 2 nb^2 naux doubles of device scratch.  Synchronised on return.  The
+ * body of the drop-in ri_ao2mo_f_ (restmatr.f90:158-194). */
+rt_status rt_ri_ao2mo_host(const double* C, const double* B, double* ri3mo, int nb, int ns, int naux, int form,
+                           int nslices, void* stream);
 
 /* rt_ri_ov_k_host for symmetric ri3ao slabs (B^P_{mu,nu} = B^P_{nu,mu}, as the
  * three-centre integrals (mu nu|P) always are): only the upper triangle of each

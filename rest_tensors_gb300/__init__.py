@@ -97,8 +97,12 @@ def lib() -> ctypes.CDLL:
     L.rt_ri_ov_k_batched.argtypes = [ctypes.POINTER(RiProblem), c_int, c_int, c_int, ctypes.POINTER(Tuning), vp]
     L.rt_ri_ov_k_host.restype = c_int
     L.rt_ri_ov_k_host.argtypes = [vp, vp, c_int, c_int, c_int, c_int, vp, vp, c_int, c_int, vp]
+    L.rt_ri_ao2mo_host.restype = c_int
+    L.rt_ri_ao2mo_host.argtypes = [vp, vp, vp, c_int, c_int, c_int, c_int, c_int, vp]
     L.rt_ri_ov_k_host_symmetric.restype = c_int
     L.rt_ri_ov_k_host_symmetric.argtypes = [vp, vp, c_int, c_int, c_int, c_int, vp, vp, c_int, c_int, vp]
+    L.rt_ri_ov_k_fp64_noalloc.restype = c_int
+    L.rt_ri_ov_k_fp64_noalloc.argtypes = [vp, vp, c_int, c_int, c_int, c_int, vp, vp, vp]
     L.rt_ri_j.restype = c_int
     L.rt_ri_j.argtypes = [vp, vp, c_int, c_int, vp, vp, vp]
     L.rt_ri_exchange_energy.restype = c_int
@@ -313,7 +317,9 @@ def _dgemm(matr_a: MatrixFull, sub_a: Tuple[range, range], opa: str,
 # --------------------------------------------------------------------------
 # Device-tensor API (torch CUDA tensors, float64)
 # --------------------------------------------------------------------------
-def _dptr(t) -> int:
+def _dptr(t, need: int = 0, name: str = "tensor") -> int:
+    """Device address of a contiguous float64 CUDA tensor on the current device holding at least
+    ``need`` elements (the extent the native call will touch); raw integer addresses pass unchecked."""
     import torch
 
     if t is None:
@@ -321,8 +327,24 @@ def _dptr(t) -> int:
     if isinstance(t, int):
         return t
     if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float64 and t.is_contiguous()):
-        raise TypeError("expected a contiguous float64 CUDA tensor")
+        raise TypeError(f"{name}: expected a contiguous float64 CUDA tensor")
+    if t.device.index != torch.cuda.current_device():
+        raise ValueError(f"{name}: tensor on cuda:{t.device.index}, current device is cuda:{torch.cuda.current_device()}")
+    if t.numel() < need:
+        raise ValueError(f"{name}: {t.numel()} elements, the call needs {need}")
     return t.data_ptr()
+
+
+def _mat_extent(ld: int, rows: int, cols: int) -> int:
+    """Elements a column-major rows x cols block with leading dimension ld spans."""
+    return 0 if rows <= 0 or cols <= 0 else (cols - 1) * ld + rows
+
+
+def _gemm_extents(opa: str, opb: str, m: int, n: int, k: int, lda: int, ldb: int, ldc: int):
+    """Elements of A, B and C that C = op(A) op(B) reads and writes (column-major, leading dimensions)."""
+    a = _mat_extent(lda, m, k) if opa in "Nn" else _mat_extent(lda, k, m)
+    b = _mat_extent(ldb, k, n) if opb in "Nn" else _mat_extent(ldb, n, k)
+    return (a if n > 0 else 0), (b if m > 0 else 0), _mat_extent(ldc, m, n)
 
 
 def _stream(stream) -> int:
@@ -341,14 +363,16 @@ def _form(form: str) -> int:
 
 
 def dgemm(opa, opb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, stream=None) -> None:
-    _check(lib().rt_dgemm(opa.encode(), opb.encode(), m, n, k, alpha, _dptr(A), lda, _dptr(B), ldb, beta, _dptr(C),
-                          ldc, _stream(stream)))
+    ea, eb, ec = _gemm_extents(opa, opb, m, n, k, lda, ldb, ldc)
+    _check(lib().rt_dgemm(opa.encode(), opb.encode(), m, n, k, alpha, _dptr(A, ea, "A"), lda, _dptr(B, eb, "B"), ldb,
+                          beta, _dptr(C, ec, "C"), ldc, _stream(stream)))
 
 
 def dgemm_split(opa, opb, m, n, k, A, lda, B, ldb, C, ldc, nslices: int = DEFAULT_NSLICES, stream=None) -> None:
     """C = op(A) op(B) in the split-precision form (float64 in and out)."""
-    _check(lib().rt_dgemm_split(opa.encode(), opb.encode(), m, n, k, _dptr(A), lda, _dptr(B), ldb, _dptr(C), ldc,
-                                nslices, _stream(stream)))
+    ea, eb, ec = _gemm_extents(opa, opb, m, n, k, lda, ldb, ldc)
+    _check(lib().rt_dgemm_split(opa.encode(), opb.encode(), m, n, k, _dptr(A, ea, "A"), lda, _dptr(B, eb, "B"), ldb,
+                                _dptr(C, ec, "C"), ldc, nslices, _stream(stream)))
 
 
 def ri_ao2mo(C, B, nb: int, ns: int, naux: int, out=None, form: str = "fp64", nslices: int = DEFAULT_NSLICES,
@@ -358,7 +382,8 @@ def ri_ao2mo(C, B, nb: int, ns: int, naux: int, out=None, form: str = "fp64", ns
 
     if out is None:
         out = torch.empty(naux * ns * ns, dtype=torch.float64, device=C.device)
-    _check(lib().rt_ri_ao2mo(_dptr(C), _dptr(B), _dptr(out), nb, ns, naux, _form(form), nslices, _stream(stream)))
+    _check(lib().rt_ri_ao2mo(_dptr(C, nb * ns, "C"), _dptr(B, nb * nb * naux, "B"), _dptr(out, naux * ns * ns, "out"),
+                             nb, ns, naux, _form(form), nslices, _stream(stream)))
     return out
 
 
@@ -371,8 +396,18 @@ def ri_ov_k(C, B, nb: int, naux: int, nocc: int, nvir: int, ov=None, K=None, for
         ov = torch.empty(nocc * nvir * naux, dtype=torch.float64, device=C.device)
     if want_k and K is None:
         K = torch.empty(nb * nb, dtype=torch.float64, device=C.device)
-    _check(lib().rt_ri_ov_k(_dptr(C), _dptr(B), nb, naux, nocc, nvir, _dptr(ov) if want_ov else None,
-                            _dptr(K) if want_k else None, _form(form), nslices, _stream(stream)))
+    _check(lib().rt_ri_ov_k(_dptr(C, nb * (nocc + nvir), "C"), _dptr(B, nb * nb * naux, "B"), nb, naux, nocc, nvir,
+                            _dptr(ov, nocc * nvir * naux, "ov") if want_ov else None,
+                            _dptr(K, nb * nb, "K") if want_k else None, _form(form), nslices, _stream(stream)))
+    return ov, K
+
+
+def ri_ov_k_fp64_noalloc(C, B, nb: int, naux: int, nocc: int, nvir: int, ov=None, K=None, stream=None):
+    """Float64 ov and K without any device allocation by the library (rt_ri_ov_k_fp64_noalloc): its scratch is
+    a fixed 32 MiB device array, so nb * nocc <= 4,194,304.  Outputs must be passed in (or None to skip)."""
+    _check(lib().rt_ri_ov_k_fp64_noalloc(_dptr(C, nb * (nocc + nvir), "C"), _dptr(B, nb * nb * naux, "B"), nb, naux,
+                                         nocc, nvir, _dptr(ov, nocc * nvir * naux, "ov"), _dptr(K, nb * nb, "K"),
+                                         _stream(stream)))
     return ov, K
 
 
@@ -386,8 +421,11 @@ def ri_ov_k_batched(problems, form: str = "split", nslices: int = DEFAULT_NSLICE
     """
     arr = (RiProblem * max(len(problems), 1))()
     for i, q in enumerate(problems):
-        arr[i] = RiProblem(_dptr(q["C"]), _dptr(q["B"]), _dptr(q.get("ov")), _dptr(q.get("K")),
-                           q["nb"], q["naux"], q["nocc"], q["nvir"])
+        nb, naux, nocc, nvir = q["nb"], q["naux"], q["nocc"], q["nvir"]
+        arr[i] = RiProblem(_dptr(q["C"], nb * (nocc + nvir), f"problem {i} C"),
+                           _dptr(q["B"], nb * nb * naux, f"problem {i} B"),
+                           _dptr(q.get("ov"), nocc * nvir * naux, f"problem {i} ov"),
+                           _dptr(q.get("K"), nb * nb, f"problem {i} K"), nb, naux, nocc, nvir)
     if isinstance(tuning, str) and tuning == "auto":
         from . import autotune
 
@@ -412,43 +450,64 @@ def ri_ov_k_host(C: np.ndarray, B: np.ndarray, nb: int, naux: int, nocc: int, nv
     _check(fn(hp(C), hp(B), nb, naux, nocc, nvir, hp(ov), hp(K), _form(form), nslices, _stream(stream)))
 
 
+def ri_ao2mo_host(C: np.ndarray, B: np.ndarray, ri3mo: np.ndarray, nb: int, ns: int, naux: int,
+                  form: str = "fp64", nslices: int = DEFAULT_NSLICES, stream=None) -> None:
+    """Host-buffer full transform (rt_ri_ao2mo_host): C [nb, ns], B [nb, nb, naux] -> ri3mo [naux, ns, ns],
+    pipelined over the host link.  Arguments are numpy arrays or raw host addresses."""
+    def hp(a, need, name):
+        if isinstance(a, np.ndarray):
+            if a.dtype != np.float64 or not (a.flags.c_contiguous or a.flags.f_contiguous):
+                raise TypeError(f"{name}: expected a contiguous float64 array")
+            if a.size < need:
+                raise ValueError(f"{name}: {a.size} elements, the call needs {need}")
+            return a.ctypes.data
+        return int(a)
+
+    _check(lib().rt_ri_ao2mo_host(hp(C, nb * ns, "C"), hp(B, nb * nb * naux, "B"), hp(ri3mo, naux * ns * ns, "ri3mo"),
+                                  nb, ns, naux, _form(form), nslices, _stream(stream)))
+
+
 def special_dgemm_01(ten3, size_a, range_x_a: range, range_z_a: range, matr_b, size_b, range_row_b: range,
                      range_column_b: range, alpha: float = 1.0, beta: float = 0.0, form: str = "fp64",
                      nslices: int = DEFAULT_NSLICES, stream=None) -> None:
     """special_dgemm_f_01 on device tensors (flat, column-major), in place on ``ten3``."""
     _check(lib().rt_special_dgemm_01(
-        _dptr(ten3), size_a[0], size_a[1], size_a[2], range_x_a.start, len(range_x_a), range_z_a.start,
-        len(range_z_a), _dptr(matr_b), size_b[0], size_b[1], range_row_b.start, len(range_row_b),
+        _dptr(ten3, size_a[0] * size_a[1] * size_a[2], "ten3_a"), size_a[0], size_a[1], size_a[2], range_x_a.start,
+        len(range_x_a), range_z_a.start, len(range_z_a), _dptr(matr_b, size_b[0] * size_b[1], "matr_b"), size_b[0],
+        size_b[1], range_row_b.start, len(range_row_b),
         range_column_b.start, len(range_column_b), alpha, beta, _form(form), nslices, _stream(stream)))
 
 
 def copy_mm(x_len: int, y_len: int, f_matr, f_size, f_start, t_matr, t_size, t_start, stream=None) -> None:
     """restmatr.f90:197-212 on device matrices: t[ts.., ..] = f[fs.., ..] for an x_len x y_len block."""
-    _check(lib().rt_copy_mm(x_len, y_len, _dptr(f_matr), f_size[0], f_size[1], f_start[0], f_start[1],
-                            _dptr(t_matr), t_size[0], t_size[1], t_start[0], t_start[1], _stream(stream)))
+    _check(lib().rt_copy_mm(x_len, y_len, _dptr(f_matr, f_size[0] * f_size[1], "f_matr"), f_size[0], f_size[1],
+                            f_start[0], f_start[1], _dptr(t_matr, t_size[0] * t_size[1], "t_matr"), t_size[0],
+                            t_size[1], t_start[0], t_start[1], _stream(stream)))
 
 
 def copy_mr(x1_len: int, x2_len: int, f_matr, f_size, f_start, t_ri, t_size, t_start, t_x3: int, mode: int,
             stream=None) -> None:
     """restmatr.f90:215-238 on device data: a matrix block into a rank-3 tensor (mode 0, 1 or 2)."""
-    _check(lib().rt_copy_mr(x1_len, x2_len, _dptr(f_matr), f_size[0], f_size[1], f_start[0], f_start[1],
-                            _dptr(t_ri), t_size[0], t_size[1], t_size[2], t_start[0], t_start[1], t_x3, mode,
-                            _stream(stream)))
+    _check(lib().rt_copy_mr(x1_len, x2_len, _dptr(f_matr, f_size[0] * f_size[1], "f_matr"), f_size[0], f_size[1],
+                            f_start[0], f_start[1], _dptr(t_ri, t_size[0] * t_size[1] * t_size[2], "t_ri"),
+                            t_size[0], t_size[1], t_size[2], t_start[0], t_start[1], t_x3, mode, _stream(stream)))
 
 
 def copy_rm(x1_len: int, x2_len: int, f_ri, f_size, f_start, f_x3: int, mode: int, t_matr, t_size, t_start,
             stream=None) -> None:
     """restmatr.f90:241-264 on device data: a rank-3 tensor block into a matrix (mode 0, 1 or 2)."""
-    _check(lib().rt_copy_rm(x1_len, x2_len, _dptr(f_ri), f_size[0], f_size[1], f_size[2], f_start[0], f_start[1],
-                            f_x3, mode, _dptr(t_matr), t_size[0], t_size[1], t_start[0], t_start[1],
-                            _stream(stream)))
+    _check(lib().rt_copy_rm(x1_len, x2_len, _dptr(f_ri, f_size[0] * f_size[1] * f_size[2], "f_ri"), f_size[0],
+                            f_size[1], f_size[2], f_start[0], f_start[1], f_x3, mode,
+                            _dptr(t_matr, t_size[0] * t_size[1], "t_matr"), t_size[0], t_size[1], t_start[0],
+                            t_start[1], _stream(stream)))
 
 
 def copy_rr(lens, f_ri, f_size, f_start, t_ri, t_size, t_start, stream=None) -> None:
     """restmatr.f90:266-285 on device data: a block between rank-3 tensors."""
-    _check(lib().rt_copy_rr(lens[0], lens[1], lens[2], _dptr(f_ri), f_size[0], f_size[1], f_size[2], f_start[0],
-                            f_start[1], f_start[2], _dptr(t_ri), t_size[0], t_size[1], t_size[2], t_start[0],
-                            t_start[1], t_start[2], _stream(stream)))
+    _check(lib().rt_copy_rr(lens[0], lens[1], lens[2], _dptr(f_ri, f_size[0] * f_size[1] * f_size[2], "f_ri"),
+                            f_size[0], f_size[1], f_size[2], f_start[0], f_start[1], f_start[2],
+                            _dptr(t_ri, t_size[0] * t_size[1] * t_size[2], "t_ri"), t_size[0], t_size[1], t_size[2],
+                            t_start[0], t_start[1], t_start[2], _stream(stream)))
 
 
 def ri_transpose(ri, size, order: str, out=None, stream=None):
@@ -457,7 +516,9 @@ def ri_transpose(ri, size, order: str, out=None, stream=None):
 
     if out is None:
         out = torch.empty(int(size[0]) * int(size[1]) * int(size[2]), dtype=torch.float64, device=ri.device)
-    _check(lib().rt_ri_transpose(_dptr(ri), size[0], size[1], size[2], order.encode(), _dptr(out), _stream(stream)))
+    nel = int(size[0]) * int(size[1]) * int(size[2])
+    _check(lib().rt_ri_transpose(_dptr(ri, nel, "ri"), size[0], size[1], size[2], order.encode(), _dptr(out, nel, "out"),
+                                 _stream(stream)))
     return out
 
 
@@ -467,7 +528,8 @@ def ri_pack_symm(ri, nao: int, naux: int, out=None, stream=None):
 
     if out is None:
         out = torch.empty(max(nao * (nao + 1) // 2 * naux, 1), dtype=torch.float64, device=ri.device)
-    _check(lib().rt_ri_pack_symm(_dptr(ri), nao, naux, _dptr(out), _stream(stream)))
+    _check(lib().rt_ri_pack_symm(_dptr(ri, nao * nao * naux, "ri"), nao, naux,
+                                 _dptr(out, nao * (nao + 1) // 2 * naux, "out"), _stream(stream)))
     return out[: nao * (nao + 1) // 2 * naux]
 
 
@@ -485,8 +547,9 @@ def newton_schulz_inverse_square_root_v02(S, n: int, threshold: float, mix_param
         out = torch.empty(n * n, dtype=torch.float64, device=S.device)
     shifts = (ctypes.c_double * len(level_shift))(*[float(x) for x in level_shift])
     conv, steps = ctypes.c_int(0), ctypes.c_int(0)
-    _check(lib().rt_newton_schulz_inv_sqrt(_dptr(S), n, threshold, mix_parameter, num_iter, shifts,
-                                           len(level_shift), _form(form), nslices, _dptr(out), ctypes.byref(conv),
+    _check(lib().rt_newton_schulz_inv_sqrt(_dptr(S, n * n, "S"), n, threshold, mix_parameter, num_iter, shifts,
+                                           len(level_shift), _form(form), nslices, _dptr(out, n * n, "out"),
+                                           ctypes.byref(conv),
                                            ctypes.byref(steps), _stream(stream)))
     return out, 0, bool(conv.value), int(steps.value)
 
@@ -498,7 +561,8 @@ def ri_j(B, D, nb: int, naux: int, w=None, J=None, stream=None):
         w = torch.empty(naux, dtype=torch.float64, device=B.device)
     if J is None:
         J = torch.empty(nb * nb, dtype=torch.float64, device=B.device)
-    _check(lib().rt_ri_j(_dptr(B), _dptr(D), nb, naux, _dptr(w), _dptr(J), _stream(stream)))
+    _check(lib().rt_ri_j(_dptr(B, nb * nb * naux, "B"), _dptr(D, nb * nb, "D"), nb, naux, _dptr(w, naux, "w"),
+                         _dptr(J, nb * nb, "J"), _stream(stream)))
     return w, J
 
 
@@ -507,7 +571,8 @@ def exchange_energy(D, K, nb: int, out=None, stream=None):
 
     if out is None:
         out = torch.empty(1, dtype=torch.float64, device=D.device)
-    _check(lib().rt_ri_exchange_energy(_dptr(D), _dptr(K), nb, _dptr(out), _stream(stream)))
+    _check(lib().rt_ri_exchange_energy(_dptr(D, nb * nb, "D"), _dptr(K, nb * nb, "K"), nb, _dptr(out, 1, "out"),
+                                       _stream(stream)))
     return out
 
 
@@ -516,7 +581,7 @@ def synth_ri3ao(seed: int, nb: int, naux: int, P0: int = 0, out=None, stream=Non
 
     if out is None:
         out = torch.empty(nb * nb * naux, dtype=torch.float64, device="cuda")
-    _check(lib().rt_synth_ri3ao(seed, nb, P0, naux, _dptr(out), _stream(stream)))
+    _check(lib().rt_synth_ri3ao(seed, nb, P0, naux, _dptr(out, nb * nb * naux, "out"), _stream(stream)))
     return out
 
 
@@ -593,7 +658,8 @@ def ri_iajb(Bov, nov: int, naux: int, M=None, form: str = "split", nslices: int 
 
     if M is None:
         M = torch.empty(nov * nov, dtype=torch.float64, device=Bov.device)
-    _check(lib().rt_ri_iajb(_dptr(Bov), nov, naux, _dptr(M), _form(form), nslices, _stream(stream)))
+    _check(lib().rt_ri_iajb(_dptr(Bov, nov * naux, "Bov"), nov, naux, _dptr(M, nov * nov, "M"), _form(form), nslices,
+                            _stream(stream)))
     return M
 
 
@@ -603,7 +669,8 @@ def ri_response_matvec(Bov, delta, nov: int, naux: int, X, nvec: int, AX=None, f
 
     if AX is None:
         AX = torch.empty(nov * nvec, dtype=torch.float64, device=Bov.device)
-    _check(lib().rt_ri_response_matvec(_dptr(Bov), _dptr(delta), nov, naux, _dptr(X), _dptr(AX), nvec, _form(form),
+    _check(lib().rt_ri_response_matvec(_dptr(Bov, nov * naux, "Bov"), _dptr(delta, nov, "delta"), nov, naux,
+                                       _dptr(X, nov * nvec, "X"), _dptr(AX, nov * nvec, "AX"), nvec, _form(form),
                                        nslices, _stream(stream)))
     return AX
 
@@ -637,8 +704,8 @@ def davidson_solve(a_x, x0_1d, hdiag, params: DavidsonParams = None, print_level
     its = ctypes.c_int(0)
     x = torch.zeros(nr * n, dtype=torch.float64, device=x0_1d.device)
     pc = params._c()
-    _check(lib().rt_davidson_solve(cfn, None, _dptr(x0_1d), _dptr(hdiag), n, ctypes.byref(pc), print_level, conv, e,
-                                   _dptr(x), ctypes.byref(its), _stream(stream)))
+    _check(lib().rt_davidson_solve(cfn, None, _dptr(x0_1d, n, "x0"), _dptr(hdiag, n, "hdiag"), n, ctypes.byref(pc),
+                                   print_level, conv, e, _dptr(x, nr * n, "x"), ctypes.byref(its), _stream(stream)))
     return [bool(c) for c in conv], list(e), x.view(nr, n), its.value
 
 
@@ -654,7 +721,8 @@ def davidson_ri_response(Bov, delta, nov: int, naux: int, x0_1d, params: Davidso
     its = ctypes.c_int(0)
     x = torch.zeros(nr * nov, dtype=torch.float64, device=Bov.device)
     pc = params._c()
-    _check(lib().rt_davidson_ri_response(_dptr(Bov), _dptr(delta), nov, naux, _form(form), nslices, _dptr(x0_1d),
+    _check(lib().rt_davidson_ri_response(_dptr(Bov, nov * naux, "Bov"), _dptr(delta, nov, "delta"), nov, naux,
+                                         _form(form), nslices, _dptr(x0_1d, nov, "x0"),
                                          ctypes.byref(pc), print_level, conv, e, _dptr(x), ctypes.byref(its),
                                          _stream(stream)))
     return [bool(c) for c in conv], list(e), x.view(nr, nov), its.value

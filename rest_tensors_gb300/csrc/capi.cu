@@ -1,7 +1,9 @@
 // capi.cu - the exported C ABI: the reference's Fortran seam (drop-in, host
 // pointers) and the rt_* device-pointer API, composed from the float64 and
 // split-precision GEMM services.
+#include <stdlib.h>
 #include <string.h>
+#include <strings.h>
 
 #include <algorithm>
 #include <atomic>
@@ -32,6 +34,42 @@ int64_t split_block(int64_t nb, int64_t naux, int S) {
     return std::max<int64_t>(1, std::min<int64_t>(blk, naux));
 }
 
+// chunks_per_item for "the whole contraction range in one work item".
+constexpr int kWholeRange = 1 << 30;
+
+// The two split-form products of the full transform.  Neither splits its
+// contraction, so a CTA's int64 range guard depends only on nb and every
+// element is the same however the slabs or columns are blocked.
+// T^P = B^P C over slabs [0, np) of B:  A(m=(mu,P), k=nu) = B[mu + nb nu + nb^2 P],
+// B(n=p, k=nu) = C[nu + nb p],  T[mu + nb p + nb ns P].
+OzGemm t_product(const double* C, const double* B, int nb, int ns, int64_t np, double* T, int S) {
+    OzGemm g;
+    g.K = nb;
+    g.A.p = B; g.A.rows = (int64_t)nb * np; g.A.div = nb;
+    g.A.s0 = 1; g.A.s1 = (int64_t)nb * nb; g.A.sk = nb;
+    g.B.p = C; g.B.rows = ns; g.B.s0 = nb; g.B.sk = 1;
+    g.C.p = T; g.C.md = nb; g.C.ms0 = 1; g.C.ms1 = (int64_t)nb * ns; g.C.ns0 = nb;
+    g.nslices = S;
+    g.chunks_per_item = kWholeRange;
+    return g;
+}
+
+// R[P + naux p + naux ns q] = sum_mu C[mu,p] T^P[mu,q] for nq columns q of T (Tq = T + nb q0) over np
+// slabs:  A(m=(q,P), k=mu) = Tq[mu + nb q + nb ns P],  B(n=p, k=mu) = C[mu + nb p],  output from Rq =
+// R + P0 + naux ns q0.
+OzGemm r_product(const double* C, const double* Tq, int nb, int ns, int64_t nq, int64_t np, int naux, double* Rq,
+                 int S) {
+    OzGemm g;
+    g.K = nb;
+    g.A.p = Tq; g.A.rows = nq * np; g.A.div = nq;
+    g.A.s0 = nb; g.A.s1 = (int64_t)nb * ns; g.A.sk = 1;
+    g.B.p = C; g.B.rows = ns; g.B.s0 = nb; g.B.sk = 1;
+    g.C.p = Rq; g.C.md = nq; g.C.ms0 = (int64_t)naux * ns; g.C.ms1 = 1; g.C.ns0 = naux;
+    g.nslices = S;
+    g.chunks_per_item = kWholeRange;
+    return g;
+}
+
 rt_status ri_ao2mo_split(const double* C, const double* B, double* R, int nb, int ns, int naux, int S,
                          cudaStream_t stream) {
     const int64_t blk = split_block(nb, naux, S);
@@ -41,31 +79,14 @@ rt_status ri_ao2mo_split(const double* C, const double* B, double* R, int nb, in
     double* T = xb.as<double>();
     for (int64_t P0 = 0; P0 < naux; P0 += blk) {
         const int64_t np = std::min<int64_t>(blk, naux - P0);
-        // T^P = B^P C: A(m=(mu,P), k=nu) = B[mu + nb nu + nb^2 P], B(n=p, k=nu) = C[nu + nb p]
-        OzGemm g1;
-        g1.K = nb;
-        g1.A.p = B + P0 * (int64_t)nb * nb; g1.A.rows = (int64_t)nb * np; g1.A.div = nb;
-        g1.A.s0 = 1; g1.A.s1 = (int64_t)nb * nb; g1.A.sk = nb;
-        g1.B.p = C; g1.B.rows = ns; g1.B.s0 = nb; g1.B.sk = 1;
-        g1.C.p = T; g1.C.md = nb; g1.C.ms0 = 1; g1.C.ms1 = per; g1.C.ns0 = nb;
-        g1.nslices = S;
-        RT_TRY(oz_gemm(g1, stream));
-        // R^P[p,q] = sum_mu C[mu,p] T^P[mu,q]: A(m=(q,P), k=mu) = T[mu + nb m], B(n=p, k=mu) = C[mu + nb p]
-        OzGemm g2;
-        g2.K = nb;
-        g2.A.p = T; g2.A.rows = (int64_t)ns * np; g2.A.s0 = nb; g2.A.sk = 1;
-        g2.B.p = C; g2.B.rows = ns; g2.B.s0 = nb; g2.B.sk = 1;
-        g2.C.p = R + P0; g2.C.md = ns; g2.C.ms0 = (int64_t)naux * ns; g2.C.ms1 = 1; g2.C.ns0 = naux;
-        g2.nslices = S;
-        RT_TRY(oz_gemm(g2, stream));
+        RT_TRY(oz_gemm(t_product(C, B + P0 * (int64_t)nb * nb, nb, ns, np, T, S), stream));
+        RT_TRY(oz_gemm(r_product(C, T, nb, ns, ns, np, naux, R + P0, S), stream));
     }
     return RT_OK;
 }
 
 // Half-transform and ov block for slabs [P0, P0 + np) of B (B already offset to slab P0):
 //   X^P = B^P C_occ  ->  X[mu + nb i + nb nocc P],   ov[i,a,P] = (X^P^T C_vir)[i,a].
-// chunks_per_item for "the whole contraction range in one work item".
-constexpr int kWholeRange = 1 << 30;
 
 // The three split-form products of the ov + RI-K path.
 // X^P = B^P C_occ:  A(m=(mu,P), k=nu) = B[mu + nb nu + nb^2 P], B(n=i, k=nu) = C[nu + nb i].
@@ -780,10 +801,202 @@ rt_status ri_ov_k_host_impl(const double* C, const double* B, int nb, int naux, 
     return error_word_check(s, "rt_ri_ov_k_host");
 }
 
+// Host-buffer full transform, pipelined over the host link.
+//   Phase 1, per slab block b: ri3ao slabs of block b arrive on the copy stream
+//   while the half-transform T^P = B^P C of block b-1 runs.
+//   Phase 2, per block of q columns: ri3mo[:, :, q0:q1] = sum_mu C[mu,p] T^P[mu,q]
+//   for every P is contiguous in the P-fastest layout, so its copy to the host
+//   overlaps the next column block's GEMM.  ri3mo reuses ri3ao's device buffer
+//   (phase 2 starts after every read of B on the same stream).
+// Every output element is computed exactly as by rt_ri_ao2mo: the column
+// blocks change which rows share a launch, not what any element sums.
+rt_status ri_ao2mo_host_impl(const double* C, const double* B, double* R, int nb, int ns, int naux, int form,
+                             int nslices, cudaStream_t s) {
+    RT_REQUIRE(nb >= 0 && ns >= 0 && naux >= 0, "ri_ao2mo host: negative dimension");
+    RT_REQUIRE(valid_form(form, nslices), "ri_ao2mo host: bad form/nslices (%d, %d)", form, nslices);
+    const size_t nR = (size_t)naux * ns * ns;
+    if (nR == 0) return RT_OK;
+    if (nb == 0) {
+        memset(R, 0, sizeof(double) * nR);
+        return RT_OK;
+    }
+    RT_REQUIRE(C && B && R, "ri_ao2mo host: null pointer");
+    const int64_t slab = (int64_t)nb * nb, per = (int64_t)nb * ns;
+    const size_t nB = (size_t)slab * naux;
+    ScratchBuf dC, dB, dT, dRx;
+    RT_TRY(scratch_alloc(dC, sizeof(double) * (size_t)per, s));
+    RT_TRY(scratch_alloc(dB, sizeof(double) * nB, s));
+    RT_TRY(scratch_alloc(dT, sizeof(double) * (size_t)per * naux, s));
+    double* dR = dB.as<double>();
+    if (nR > nB) {
+        RT_TRY(scratch_alloc(dRx, sizeof(double) * nR, s));
+        dR = dRx.as<double>();
+    }
+    RT_TRY(error_word_reset(s));
+    // ~512 MB per slab block and per ri3mo column block.
+    const int64_t sblk = std::max<int64_t>(1, std::min<int64_t>(naux, ((int64_t)64 << 20) / std::max<int64_t>(slab, 1)));
+    const int64_t qcol = (int64_t)naux * ns;  // elements of one ri3mo column q
+    const int64_t qblk = std::max<int64_t>(1, std::min<int64_t>(ns, ((int64_t)64 << 20) / std::max<int64_t>(qcol, 1)));
+    const int64_t nsb = ceil_div(naux, sblk), nqb = ceil_div(ns, qblk);
+    cudaStream_t hs = nullptr, ds = nullptr;
+    cudaEvent_t ready = nullptr;
+    std::vector<cudaEvent_t> in(nsb, nullptr), out(nqb, nullptr);
+    rt_status st = RT_OK;
+    auto fail = [&](cudaError_t e, const char* what) {
+        set_error(RT_ERR_CUDA, "ri_ao2mo host: %s: %s", what, cudaGetErrorString(e));
+        st = RT_ERR_CUDA;
+    };
+    cudaError_t e;
+    if ((e = cudaStreamCreateWithFlags(&hs, cudaStreamNonBlocking)) != cudaSuccess) fail(e, "stream");
+    if (st == RT_OK && (e = cudaStreamCreateWithFlags(&ds, cudaStreamNonBlocking)) != cudaSuccess) fail(e, "stream");
+    if (st == RT_OK && (e = cudaEventCreateWithFlags(&ready, cudaEventDisableTiming)) != cudaSuccess) fail(e, "event");
+    for (int64_t b = 0; st == RT_OK && b < nsb; ++b)
+        if ((e = cudaEventCreateWithFlags(&in[b], cudaEventDisableTiming)) != cudaSuccess) fail(e, "event");
+    for (int64_t j = 0; st == RT_OK && j < nqb; ++j)
+        if ((e = cudaEventCreateWithFlags(&out[j], cudaEventDisableTiming)) != cudaSuccess) fail(e, "event");
+    if (st == RT_OK && (e = cudaMemcpyAsync(dC.p, C, sizeof(double) * (size_t)per, cudaMemcpyHostToDevice, s)) !=
+                           cudaSuccess)
+        fail(e, "host-to-device copy");
+    if (st == RT_OK) {
+        // The pool allocations above are ordered on `s`; the copy streams start after them.
+        cudaEventRecord(ready, s);
+        cudaStreamWaitEvent(hs, ready, 0);
+        cudaStreamWaitEvent(ds, ready, 0);
+        const double* Cd = dC.as<double>();
+        auto half = [&](int64_t b) -> rt_status {
+            const int64_t P0 = b * sblk, np = std::min<int64_t>(sblk, naux - P0);
+            cudaStreamWaitEvent(s, in[b], 0);
+            const double* Bb = dB.as<double>() + P0 * slab;
+            double* Tb = dT.as<double>() + P0 * per;
+            if (form == RT_FORM_FP64) {
+                GemmF64 g1;
+                g1.opa = 'N'; g1.opb = 'N'; g1.m = nb; g1.n = ns; g1.k = nb;
+                g1.A = Bb; g1.lda = nb; g1.sA = slab;
+                g1.B = Cd; g1.ldb = nb; g1.sB = 0;
+                g1.C = Tb; g1.rsC = 1; g1.csC = nb; g1.bsC = per; g1.batch = np;
+                return gemm_f64(g1, s);
+            }
+            return oz_gemm(t_product(Cd, Bb, nb, ns, np, Tb, nslices), s);
+        };
+        for (int64_t b = 0; st == RT_OK && b < nsb; ++b) {
+            const int64_t P0 = b * sblk, np = std::min<int64_t>(sblk, naux - P0);
+            st = copy_slabs_h2d(B + P0 * slab, dB.as<double>() + P0 * slab, np * slab, hs);
+            if (st != RT_OK) break;
+            cudaEventRecord(in[b], hs);
+            if (b > 0) st = half(b - 1);
+        }
+        if (st == RT_OK) st = half(nsb - 1);
+        auto second = [&](int64_t j) -> rt_status {
+            const int64_t q0 = j * qblk, nq = std::min<int64_t>(qblk, ns - q0);
+            double* Rq = dR + qcol * q0;
+            const double* Tq = dT.as<double>() + (int64_t)nb * q0;
+            if (form == RT_FORM_FP64) {
+                GemmF64 g2;
+                g2.opa = 'T'; g2.opb = 'N'; g2.m = ns; g2.n = nq; g2.k = nb;
+                g2.A = Cd; g2.lda = nb; g2.sA = 0;
+                g2.B = Tq; g2.ldb = nb; g2.sB = per;
+                g2.C = Rq; g2.rsC = naux; g2.csC = qcol; g2.bsC = 1; g2.batch = naux;
+                return gemm_f64(g2, s);
+            }
+            return oz_gemm(r_product(Cd, Tq, nb, ns, nq, naux, naux, Rq, nslices), s);
+        };
+        // Each column block's copy is queued after the next block's GEMM, so a copy to
+        // pageable memory (which returns only when done) still overlaps device work.
+        for (int64_t j = 0; st == RT_OK && j <= nqb; ++j) {
+            if (j < nqb) {
+                st = second(j);
+                if (st != RT_OK) break;
+                cudaEventRecord(out[j], s);
+            }
+            if (j > 0) {
+                const int64_t q0 = (j - 1) * qblk, nq = std::min<int64_t>(qblk, ns - q0);
+                cudaStreamWaitEvent(ds, out[j - 1], 0);
+                if ((e = cudaMemcpyAsync(R + qcol * q0, dR + qcol * q0, sizeof(double) * (size_t)(qcol * nq),
+                                         cudaMemcpyDeviceToHost, ds)) != cudaSuccess)
+                    fail(e, "device-to-host copy");
+            }
+        }
+    }
+    if (hs) cudaStreamSynchronize(hs);
+    if (ds) cudaStreamSynchronize(ds);
+    cudaStreamSynchronize(s);
+    for (auto ev : in) if (ev) cudaEventDestroy(ev);
+    for (auto ev : out) if (ev) cudaEventDestroy(ev);
+    if (ready) cudaEventDestroy(ready);
+    if (hs) cudaStreamDestroy(hs);
+    if (ds) cudaStreamDestroy(ds);
+    if (st != RT_OK) return st;
+    return error_word_check(s, "ri_ao2mo host");
+}
+
+// Precision form of the Fortran-ABI drop-ins, read once per process from the
+// environment: RT_FORM = fp64 (default) | split, RT_NSLICES = 3..8 (default 7).
+// Unchanged callers therefore keep float64 parity; a deployment opts in to the
+// split form without relinking.  An unrecognised value makes every drop-in call
+// fail (rt_last_status) rather than silently run another form.
+struct SeamForm {
+    int form = RT_FORM_FP64;
+    int nslices = 7;
+    bool ok = true;
+    char why[160] = {0};
+};
+
+const SeamForm& seam_form() {
+    static const SeamForm f = [] {
+        SeamForm r;
+        if (const char* v = getenv("RT_FORM")) {
+            if (!strcasecmp(v, "split")) r.form = RT_FORM_SPLIT;
+            else if (strcasecmp(v, "fp64") && *v) {
+                r.ok = false;
+                snprintf(r.why, sizeof(r.why), "RT_FORM=%s: expected fp64 or split", v);
+            }
+        }
+        if (const char* v = getenv("RT_NSLICES")) {
+            char* end = nullptr;
+            const long n = strtol(v, &end, 10);
+            if (*v && end && *end == 0 && n >= 3 && n <= 8) r.nslices = (int)n;
+            else if (*v) {
+                r.ok = false;
+                snprintf(r.why, sizeof(r.why), "RT_NSLICES=%s: expected an integer in 3..8", v);
+            }
+        }
+        return r;
+    }();
+    return f;
+}
+
+rt_status seam_check(const char* who) {
+    const SeamForm& f = seam_form();
+    if (!f.ok) {
+        set_error(RT_ERR_INVALID_ARG, "%s: %s", who, f.why);
+        return RT_ERR_INVALID_ARG;
+    }
+    return RT_OK;
+}
+
+// C block <- alpha * P + beta * C block (column-major, leading dimension ldc;
+// beta == 0 does not read C).
+__global__ void __launch_bounds__(256) axpby_block_kernel(double* __restrict__ Cb, int64_t ldc,
+                                                          const double* __restrict__ P, int64_t m, int64_t n,
+                                                          double alpha, double beta) {
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < m * n;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = idx % m, j = idx / m;
+        double* c = Cb + i + j * ldc;
+        *c = beta == 0.0 ? alpha * P[idx] : fma(beta, *c, alpha * P[idx]);
+    }
+}
+
 }  // namespace
 }  // namespace rt
 
 extern "C" {
+
+rt_status rt_ri_ao2mo_host(const double* C, const double* B, double* ri3mo, int nb, int ns, int naux, int form,
+                           int nslices, void* stream) {
+    NvtxRange nvtx_range("rt_ri_ao2mo_host");
+    return ri_ao2mo_host_impl(C, B, ri3mo, nb, ns, naux, form, nslices, (cudaStream_t)stream);
+}
 
 rt_status rt_ri_ov_k_host(const double* C, const double* B, int nb, int naux, int nocc, int nvir, double* ov,
                           double* K, int form, int nslices, void* stream) {
@@ -804,25 +1017,20 @@ void ri_ao2mo_f_(const double* eigenvector, const double* ri3fn, double* ri3mo, 
     NvtxRange nvtx_range("ri_ao2mo_f_");
     rt::set_error(RT_OK, "");
     const int ns = *num_states, nb = *num_basis, naux = *num_auxbas;
-    const size_t nR = (size_t)naux * ns * ns;
-    if (nR) memset(ri3mo, 0, sizeof(double) * nR);
-    if (ns <= 0 || nb <= 0 || naux <= 0) return;
-    cudaStream_t s = cudaStreamPerThread;
-    const size_t nC = (size_t)nb * ns, nB = (size_t)nb * nb * naux;
+    const size_t nR = (ns > 0 && naux > 0) ? (size_t)naux * ns * ns : 0;
     auto run = [&]() -> rt_status {
-        ScratchBuf dC, dB, dR;
-        RT_TRY(scratch_alloc(dC, sizeof(double) * nC, s));
-        RT_TRY(scratch_alloc(dB, sizeof(double) * nB, s));
-        RT_TRY(scratch_alloc(dR, sizeof(double) * nR, s));
-        RT_CUDA_TRY(cudaMemcpyAsync(dC.p, eigenvector, sizeof(double) * nC, cudaMemcpyHostToDevice, s));
-        RT_CUDA_TRY(cudaMemcpyAsync(dB.p, ri3fn, sizeof(double) * nB, cudaMemcpyHostToDevice, s));
-        RT_TRY(rt_ri_ao2mo(dC.as<double>(), dB.as<double>(), dR.as<double>(), nb, ns, naux, RT_FORM_FP64, 0, s));
-        RT_CUDA_TRY(cudaMemcpyAsync(ri3mo, dR.p, sizeof(double) * nR, cudaMemcpyDeviceToHost, s));
-        RT_CUDA_TRY(cudaStreamSynchronize(s));
-        return RT_OK;
+        RT_TRY(seam_check("ri_ao2mo_f_"));
+        if (nR == 0) return RT_OK;
+        if (nb <= 0) {
+            memset(ri3mo, 0, sizeof(double) * nR);
+            return RT_OK;
+        }
+        const SeamForm& f = seam_form();
+        return ri_ao2mo_host_impl(eigenvector, ri3fn, ri3mo, nb, ns, naux, f.form, f.nslices, cudaStreamPerThread);
     };
     if (run() != RT_OK) {
-        memset(ri3mo, 0, sizeof(double) * nR);
+        // The Fortran zero-fills ri3mo first (restmatr.f90:178): a failed call leaves that state.
+        if (nR) memset(ri3mo, 0, sizeof(double) * nR);
         fprintf(stderr, "ri_ao2mo_f_: %s\n", rt_last_error());
     }
 }
@@ -855,8 +1063,10 @@ void general_dgemm_f_(const double* matr_a, const int* rows_a, const int* column
         RT_REQUIRE(*start_row_c >= 0 && *start_row_c + m <= *rows_c && *start_column_c >= 0 &&
                        *start_column_c + n <= *columns_c,
                    "general_dgemm_f_: block of C outside the matrix");
+        RT_TRY(seam_check("general_dgemm_f_"));
         if (m == 0 || n == 0) return RT_OK;
         cudaStream_t s = cudaStreamPerThread;
+        const SeamForm& f = seam_form();
         const int ra = std::max(*len_row_a, 1), rb = std::max(*len_row_b, 1);
         ScratchBuf dA, dB, dC;
         RT_TRY(scratch_alloc(dA, sizeof(double) * (size_t)ra * std::max(*len_column_a, 1), s));
@@ -875,6 +1085,21 @@ void general_dgemm_f_(const double* matr_a, const int* rows_a, const int* column
         double* cblk = matr_c + (size_t)*start_column_c * *rows_c + *start_row_c;
         RT_CUDA_TRY(cudaMemcpy2DAsync(dC.p, sizeof(double) * m, cblk, sizeof(double) * *rows_c, sizeof(double) * m,
                                       n, cudaMemcpyHostToDevice, s));
+        if (f.form == RT_FORM_SPLIT) {
+            // The product in the split form, then C <- alpha * P + beta * C in float64.
+            ScratchBuf dP;
+            RT_TRY(scratch_alloc(dP, sizeof(double) * (size_t)m * n, s));
+            RT_TRY(rt_dgemm_split(oa, ob, m, n, k, dA.as<double>(), ra, dB.as<double>(), rb, dP.as<double>(), m,
+                                  f.nslices, s));
+            const int64_t total = (int64_t)m * n;
+            axpby_block_kernel<<<(unsigned)std::min<int64_t>(ceil_div(total, 256), 4 * sm_count()), 256, 0, s>>>(
+                dC.as<double>(), m, dP.as<double>(), m, n, *alpha, *beta);
+            RT_TRY(check_launch("axpby_block_kernel"));
+            RT_CUDA_TRY(cudaMemcpy2DAsync(cblk, sizeof(double) * *rows_c, dC.p, sizeof(double) * m,
+                                          sizeof(double) * m, n, cudaMemcpyDeviceToHost, s));
+            RT_CUDA_TRY(cudaStreamSynchronize(s));
+            return RT_OK;
+        }
         RT_TRY(rt_dgemm(oa, ob, m, n, k, *alpha, dA.as<double>(), ra, dB.as<double>(), rb, *beta, dC.as<double>(),
                         m, s));
         RT_CUDA_TRY(cudaMemcpy2DAsync(cblk, sizeof(double) * *rows_c, dC.p, sizeof(double) * m, sizeof(double) * m,
@@ -905,8 +1130,10 @@ void special_dgemm_f_01_(double* ten3_a, const int* x_a, const int* y_a, const i
                    "special_dgemm_f_01_: block of matr_b outside the matrix");
         RT_REQUIRE(*len_row_b == lz && *len_column_b == lz,
                    "special_dgemm_f_01_: the block of matr_b must be len_z_a x len_z_a");
+        RT_TRY(seam_check("special_dgemm_f_01_"));
         if ((int64_t)lx * Y * lz == 0) return RT_OK;
         cudaStream_t s = cudaStreamPerThread;
+        const SeamForm& f = seam_form();
         const size_t blk_elems = (size_t)lx * Y * lz;
         ScratchBuf dT, dM;
         RT_TRY(scratch_alloc(dT, sizeof(double) * blk_elems, s));
@@ -923,7 +1150,7 @@ void special_dgemm_f_01_(double* ten3_a, const int* x_a, const int* y_a, const i
                                       matr_b + (size_t)*start_column_b * *rows_b + *start_row_b,
                                       sizeof(double) * *rows_b, sizeof(double) * lz, lz, cudaMemcpyHostToDevice, s));
         RT_TRY(special_dgemm_01(dT.as<double>(), lx, Y, 0, lx, 0, lz, dM.as<double>(), lz, 0, 0, *alpha, *beta,
-                                RT_FORM_FP64, 0, s));
+                                f.form, f.nslices, s));
         cudaMemcpy3DParms down = {};
         down.srcPtr = up.dstPtr;
         down.dstPtr = up.srcPtr;

@@ -20,7 +20,9 @@
 // reference's `a_x` closure), one block of vectors per call.  Vector algebra
 // is float64 on the device with fixed-order reductions; the subspace
 // eigenproblem (order <= a few dozen) is solved in float64 on the host by
-// cyclic Jacobi rotations (Golub & Van Loan, Matrix Computations, 8.5).
+// Householder tridiagonalisation and implicit QR with Wilkinson shifts (Golub &
+// Van Loan, Matrix Computations, Algorithms 8.3.1 and 8.3.3), with cyclic
+// Jacobi rotations (8.5) as the fallback.
 #include <math.h>
 #include <stdio.h>
 #include <string.h>

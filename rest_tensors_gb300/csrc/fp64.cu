@@ -665,11 +665,10 @@ rt_status ri_ov_k_fp64(const double* C, const double* B, int nb, int naux, int n
 // ---------------------------------------------------------------------------
 // Allocation-free float64 ov transform + RI-K.
 //
-// For callers that cannot allocate device memory while they run: code that
-// executes inside a CUDA stream capture that must not contain allocation
-// nodes, hosts that hand the GPU's memory to a fixed arena managed by another
-// runtime, or deployments where any cudaMalloc/cudaFree (with its implicit
-// device synchronisation) is forbidden on the serving path.  The half-
+// For callers that cannot allocate device memory while they run: hosts that
+// hand the GPU's memory to a fixed arena managed by another runtime, or
+// deployments where any cudaMalloc/cudaFree (with its implicit device
+// synchronisation) is forbidden on the serving path.  The half-
 // transform X^P = B^P C_occ lives in a fixed file-scope device array instead
 // of scratch from the memory pool, and the aux slabs stream through it in
 // blocks; K accumulates across blocks with beta = 1.  Nothing in the array

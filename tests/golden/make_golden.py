@@ -105,8 +105,9 @@ def extract(ref: str) -> dict:
 
 
 if __name__ == "__main__":
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    data = extract(ref)
+    if len(sys.argv) != 2:
+        sys.exit("usage: python make_golden.py <path of the reference checkout>")
+    data = extract(sys.argv[1])
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_doctests.json")
     with open(dst, "w") as f:
         json.dump(data, f, indent=1)

@@ -39,7 +39,7 @@ def test_header_declares_the_seam():
     names = declared_functions()
     for n in ["ri_ao2mo_f_", "general_dgemm_f_", "special_dgemm_f_01_", "rt_ri_ov_k", "rt_ri_ao2mo", "rt_ri_j",
               "rt_dgemm", "rt_special_dgemm_01", "rt_copy_rr", "rt_ri_transpose", "rt_ri_pack_symm",
-              "rt_newton_schulz_inv_sqrt"]:
+              "rt_newton_schulz_inv_sqrt", "rt_ri_ao2mo_host"]:
         assert n in names
 
 
@@ -134,3 +134,22 @@ def test_newton_schulz_rejects_bad_arguments():
     assert call(0, 1, 0, 7) == 1  # empty matrix
     assert call(4, 1, 1, 9) == 1  # split form, bad slice count
     assert call(4, 1, 0, 7) == 1  # null pointers
+
+
+@pytest.mark.parametrize("env", [{"RT_FORM": "single"}, {"RT_NSLICES": "9"}, {"RT_FORM": "split", "RT_NSLICES": "x"}])
+def test_seam_refuses_an_unknown_form_before_any_device_work(env):
+    # The seam's form is read once per process, so each setting runs in a fresh interpreter.
+    import subprocess
+    import sys
+
+    code = ("import numpy as np, rest_tensors_gb300 as rt\n"
+            "out = np.ones(2 * 2 * 3)\n"
+            "try:\n"
+            "    rt.ri_ao2mo_f(np.ones(4), np.ones(12), out, 2, 2, 3)\n"
+            "except rt.RTError as e:\n"
+            "    assert e.status == 1 and b'RT_' in rt.lib().rt_last_error(), e\n"
+            "    assert not out.any()\n"
+            "    print('refused')\n")
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, env={**os.environ, **env}, capture_output=True,
+                       text=True, timeout=120)
+    assert r.returncode == 0 and "refused" in r.stdout, r.stderr

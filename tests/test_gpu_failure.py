@@ -90,3 +90,17 @@ def test_wait_budget_is_validated():
         rt.debug_wait_timeout(-1)
     with pytest.raises(rt.RTError):
         rt.debug_wait_timeout(3_000_000_000)
+
+
+def test_wrappers_refuse_undersized_or_host_tensors():
+    # An undersized output is refused in Python, before any kernel could write past its end.
+    nb, naux, nocc, nvir = 16, 4, 3, 13
+    C = rt.synth_coef(0, nb)
+    B = rt.synth_ri3ao(0, nb, naux)
+    K = torch.empty(nb * nb - 1, dtype=torch.float64, device="cuda")
+    with pytest.raises(ValueError, match="K"):
+        rt.ri_ov_k(C, B, nb, naux, nocc, nvir, K=K)
+    with pytest.raises(ValueError, match="B"):
+        rt.ri_j(B[:-1], torch.zeros(nb * nb, dtype=torch.float64, device="cuda"), nb, naux)
+    with pytest.raises(TypeError):
+        rt.ri_ov_k(C.cpu(), B, nb, naux, nocc, nvir)
