@@ -11,6 +11,7 @@
 #include <mutex>
 
 #include "rt_internal.cuh"
+#include "rt_ptx.cuh"
 #include "../../include/rt_synth.h"
 
 namespace rt {
@@ -506,6 +507,143 @@ __global__ void __launch_bounds__(256) rij_j_kernel_scalar(const double* __restr
     J[e] = a0 + a1;
 }
 
+// One-pass RI-J: w_P = <B^P, D> and J = sum_P w_P B^P with one HBM read of B.
+//
+// A cooperative persistent grid of G CTAs (all co-resident); CTA c owns the
+// element range [c * chunk2, (c + 1) * chunk2) of every slab (in double2 units)
+// and keeps that part of J and of D in registers.  Slabs go in groups of S:
+//   * dot of group g: each CTA's partial <B^P, D> over its range, a fixed-order
+//     tree inside the CTA, is stored in partials[P][c]; then counts[g] += 1;
+//   * L groups later, J of group q = g - L: once counts[q] == G (a bounded wait),
+//     every CTA forms w_P = sum_c partials[P][c] in the same fixed order and adds
+//     w_P * B^P over its range, re-reading the slabs, which L2 still holds.
+// Deadlock-free because the dot of group g never waits: a CTA only waits for
+// dots of earlier groups, which every co-resident CTA reaches first.  Results
+// are bitwise reproducible (fixed reduction orders, one thread per J element).
+constexpr int RIJ1_THREADS = 512;
+constexpr int RIJ1_WARPS = RIJ1_THREADS / 32;
+
+struct Rij1Args {
+    const double2* B;  // slab P at B + P * n2h
+    const double2* D;
+    int64_t n2h;       // elements of one slab / 2
+    int naux;
+    int64_t chunk2;    // double2 per CTA
+    int ngroups;
+    double* w;
+    double2* J;
+    double* partials;  // [naux][G]
+    int* counts;       // [ngroups], zero on entry
+    unsigned int* err;
+};
+
+template <int S, int K2, int L>
+__global__ void __launch_bounds__(RIJ1_THREADS, 1) rij_onepass_kernel(Rij1Args a) {
+    __shared__ double red[RIJ1_WARPS][S];
+    __shared__ double ws[S];
+    __shared__ int abort_flag;
+    const int G = gridDim.x, c = blockIdx.x;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int64_t e0 = (int64_t)c * a.chunk2;
+    const int64_t e1 = min(a.n2h, e0 + a.chunk2);
+    // This thread's elements: e0 + tid + RIJ1_THREADS * k for k < K2 (those below e1).
+    const int64_t my0 = e0 + tid;
+    const int nk = my0 < e1 ? (int)min((int64_t)K2, (e1 - my0 + RIJ1_THREADS - 1) / RIJ1_THREADS) : 0;
+    double2 d[K2], jacc[K2];
+#pragma unroll
+    for (int k = 0; k < K2; ++k) {
+        d[k] = k < nk ? a.D[my0 + (int64_t)RIJ1_THREADS * k] : make_double2(0.0, 0.0);
+        jacc[k] = make_double2(0.0, 0.0);
+    }
+    if (tid == 0) abort_flag = 0;
+    __syncthreads();
+    for (int g = 0; g < a.ngroups + L; ++g) {
+        if (g < a.ngroups) {
+            const int P0 = g * S;
+            double2 x[S][K2];
+#pragma unroll
+            for (int s = 0; s < S; ++s)
+#pragma unroll
+                for (int k = 0; k < K2; ++k)
+                    x[s][k] = (P0 + s < a.naux && k < nk)
+                                  ? a.B[(int64_t)(P0 + s) * a.n2h + my0 + (int64_t)RIJ1_THREADS * k]
+                                  : make_double2(0.0, 0.0);
+            double acc[S];
+#pragma unroll
+            for (int s = 0; s < S; ++s) {
+                acc[s] = 0.0;
+#pragma unroll
+                for (int k = 0; k < K2; ++k) acc[s] = fma(x[s][k].y, d[k].y, fma(x[s][k].x, d[k].x, acc[s]));
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) acc[s] += __shfl_xor_sync(0xffffffffu, acc[s], o);
+            }
+            if (lane == 0) {
+#pragma unroll
+                for (int s = 0; s < S; ++s) red[warp][s] = acc[s];
+            }
+            __syncthreads();
+            if (tid < S && P0 + tid < a.naux) {
+                double t = 0.0;
+#pragma unroll
+                for (int w = 0; w < RIJ1_WARPS; ++w) t += red[w][tid];
+                a.partials[(int64_t)(P0 + tid) * G + c] = t;
+                __threadfence();
+            }
+            __syncthreads();
+            if (tid == 0) atomicAdd(&a.counts[g], 1);
+        }
+        if (g >= L) {
+            const int q = g - L, Q0 = q * S;
+            if (tid == 0) {
+                volatile int* cnt = a.counts + q;
+                if (*cnt < G) {
+                    const long long t0 = clock64();
+                    while (*cnt < G) {
+                        if (clock64() - t0 > ptx::kWaitCycles) {
+                            atomicOr(a.err, DEV_ERR_TIMEOUT);
+                            abort_flag = 1;
+                            break;
+                        }
+                    }
+                }
+                __threadfence();
+            }
+            __syncthreads();
+            if (abort_flag) return;
+            if (warp < S) {
+                double t = 0.0;
+                if (Q0 + warp < a.naux)
+                    for (int cc = lane; cc < G; cc += 32) t += __ldcg(a.partials + (int64_t)(Q0 + warp) * G + cc);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+                if (lane == 0) ws[warp] = t;
+            }
+            __syncthreads();
+            if (c == 0 && tid < S && Q0 + tid < a.naux && a.w) a.w[Q0 + tid] = ws[tid];
+            double2 y[S][K2];
+#pragma unroll
+            for (int s = 0; s < S; ++s)
+#pragma unroll
+                for (int k = 0; k < K2; ++k)
+                    y[s][k] = (Q0 + s < a.naux && k < nk)
+                                  ? a.B[(int64_t)(Q0 + s) * a.n2h + my0 + (int64_t)RIJ1_THREADS * k]
+                                  : make_double2(0.0, 0.0);
+#pragma unroll
+            for (int s = 0; s < S; ++s) {
+                const double wv = ws[s];
+#pragma unroll
+                for (int k = 0; k < K2; ++k) {
+                    jacc[k].x = fma(wv, y[s][k].x, jacc[k].x);
+                    jacc[k].y = fma(wv, y[s][k].y, jacc[k].y);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < K2; ++k)
+        if (k < nk) a.J[my0 + (int64_t)RIJ1_THREADS * k] = jacc[k];
+}
+
 // -tr(D K) with one CTA and a fixed reduction tree (bitwise reproducible).
 __global__ void __launch_bounds__(1024) exchange_kernel(const double* __restrict__ D, const double* __restrict__ K,
                                                         int64_t n2, double* __restrict__ out) {
@@ -546,6 +684,93 @@ __global__ void synth_kernel(uint64_t seed, int nb, int P0, int64_t total, doubl
 
 }  // namespace
 
+template <int S, int K2>
+cudaError_t launch_rij1(const Rij1Args& a, int G, cudaStream_t stream) {
+    void* args[] = {const_cast<Rij1Args*>(&a)};
+    return cudaLaunchCooperativeKernel((const void*)rij_onepass_kernel<S, K2, 1>, dim3((unsigned)G),
+                                       dim3(RIJ1_THREADS), args, 0, stream);
+}
+
+// S slabs per group for K2 double2 per thread and slab, S * K2 <= 16.
+template <int K2>
+cudaError_t launch_rij1_s(const Rij1Args& a, int S, int G, cudaStream_t stream) {
+    if constexpr (8 * K2 <= 16) {
+        if (S >= 8) return launch_rij1<8, K2>(a, G, stream);
+    }
+    if constexpr (4 * K2 <= 16) {
+        if (S >= 4) return launch_rij1<4, K2>(a, G, stream);
+    }
+    if constexpr (2 * K2 <= 16) {
+        if (S >= 2) return launch_rij1<2, K2>(a, G, stream);
+    }
+    return launch_rij1<1, K2>(a, G, stream);
+}
+
+// The one-pass form when the layout suits it (even slab length, 16-byte aligned
+// slabs, at most 16 double2 per thread and slab); `done` tells the caller
+// whether it ran.  Slabs per group: at most 8, two groups within ~48 MB so the
+// re-read of the lagging group still hits L2, and at most 16 double2 of slab
+// data per thread and group (no register spills at 512 threads).
+rt_status ri_j_onepass(const double* B, const double* D, int64_t n2, int naux, double* w, double* J,
+                       cudaStream_t stream, bool& done) {
+    done = false;
+    if ((n2 & 1) || ((uintptr_t)B & 15) || ((uintptr_t)D & 15) || ((uintptr_t)J & 15) || naux <= 0) return RT_OK;
+    const int64_t n2h = n2 / 2;
+    const int G = (int)std::max<int64_t>(1, std::min<int64_t>(sm_count(), ceil_div(n2h, RIJ1_THREADS)));
+    const int64_t chunk2 = ceil_div(n2h, G);
+    const int64_t need = ceil_div(chunk2, RIJ1_THREADS);
+    static const int kK2[] = {1, 2, 3, 4, 6, 8, 12, 16};
+    int K2 = 0;
+    for (int k : kK2)
+        if (!K2 && k >= need) K2 = k;
+    if (!K2) return RT_OK;
+    const int64_t slab_bytes = 16 * n2h;
+    int64_t smax = std::min<int64_t>({8, std::max<int64_t>(1, ((int64_t)24 << 20) / slab_bytes), 16 / K2});
+    int S = 1;
+    while (S * 2 <= smax) S *= 2;
+    const int ngroups = (int)ceil_div(naux, S);
+    ScratchBuf sb;
+    const size_t pbytes = align_up(sizeof(double) * (size_t)naux * G, 256);
+    RT_TRY(scratch_alloc(sb, pbytes + sizeof(int) * (size_t)ngroups, stream));
+    int* counts = reinterpret_cast<int*>(sb.as<uint8_t>() + pbytes);
+    RT_CUDA_TRY(cudaMemsetAsync(counts, 0, sizeof(int) * (size_t)ngroups, stream));
+    unsigned int* err = error_word_device();
+    RT_REQUIRE(err != nullptr, "ri_j: device error word unavailable");
+    Rij1Args a;
+    a.B = reinterpret_cast<const double2*>(B);
+    a.D = reinterpret_cast<const double2*>(D);
+    a.n2h = n2h;
+    a.naux = naux;
+    a.chunk2 = chunk2;
+    a.ngroups = ngroups;
+    a.w = w;
+    a.J = reinterpret_cast<double2*>(J);
+    a.partials = sb.as<double>();
+    a.counts = counts;
+    a.err = err;
+    prof_begin(PROF_RIJ, stream);
+    cudaError_t e;
+    switch (K2) {
+        case 1: e = launch_rij1_s<1>(a, S, G, stream); break;
+        case 2: e = launch_rij1_s<2>(a, S, G, stream); break;
+        case 3: e = launch_rij1_s<3>(a, S, G, stream); break;
+        case 4: e = launch_rij1_s<4>(a, S, G, stream); break;
+        case 6: e = launch_rij1_s<6>(a, S, G, stream); break;
+        case 8: e = launch_rij1_s<8>(a, S, G, stream); break;
+        case 12: e = launch_rij1_s<12>(a, S, G, stream); break;
+        default: e = launch_rij1_s<16>(a, S, G, stream); break;
+    }
+    if (e == cudaErrorCooperativeLaunchTooLarge || e == cudaErrorNotSupported) {
+        cudaGetLastError();  // not co-residable here: the two-pass kernels run instead
+        return RT_OK;
+    }
+    RT_CUDA_TRY(e);
+    prof_end(PROF_RIJ, stream, 16.0 * (double)n2h * naux);
+    RT_TRY(check_launch("rij_onepass_kernel"));
+    done = true;
+    return RT_OK;
+}
+
 rt_status ri_j_fp64(const double* B, const double* D, int nb, int naux, double* w, double* J,
                     cudaStream_t stream) {
     const int64_t n2 = (int64_t)nb * nb;
@@ -553,6 +778,11 @@ rt_status ri_j_fp64(const double* B, const double* D, int nb, int naux, double* 
     if (!w) {
         RT_TRY(scratch_alloc(wbuf, sizeof(double) * (size_t)naux, stream));
         w = wbuf.as<double>();
+    }
+    if (J) {
+        bool done = false;
+        RT_TRY(ri_j_onepass(B, D, n2, naux, w, J, stream, done));
+        if (done) return RT_OK;
     }
     rij_w_kernel<<<(unsigned)naux, 256, 0, stream>>>(B, D, n2, naux, w);
     RT_TRY(check_launch("rij_w_kernel"));

@@ -177,7 +177,10 @@ def test_empty_and_degenerate_shapes():
 
 
 # ------------------------------------------------------------ J and E_x --
-@pytest.mark.parametrize("nb,naux", [(20, 12), (33, 7), (100, 400), (40, 1100)])
+# One-pass RI-J variants by shape: (20, 12) one CTA; (100, 400) and (40, 1100) groups of 8 slabs;
+# (600, 96) 3 double2 per thread in groups of 4; (750, 33) 4 per thread with a short last group;
+# (1200, 20) 12 per thread, one slab per group; (33, 7) odd slab length: the two-pass kernels.
+@pytest.mark.parametrize("nb,naux", [(20, 12), (33, 7), (100, 400), (40, 1100), (600, 96), (750, 33), (1200, 20)])
 def test_ri_j_matches_oracle(nb, naux):
     C, B = inputs(nb, naux, seed=1)
     D = np.asfortranarray(C[:, :5] @ C[:, :5].T)
@@ -185,6 +188,8 @@ def test_ri_j_matches_oracle(nb, naux):
     w, J = rt.ri_j(dev(B), dev(D), nb, naux)
     assert relerr(w.cpu().numpy(), w_ref) < 1e-12
     assert relerr(host(J, (nb, nb)), J_ref) < 1e-12
+    w2, J2 = rt.ri_j(dev(B), dev(D), nb, naux)  # fixed reduction orders: bitwise repeatable
+    assert torch.equal(w, w2) and torch.equal(J, J2)
 
 
 @pytest.mark.parametrize("form", ["fp64", "split"])

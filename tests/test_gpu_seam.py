@@ -85,8 +85,7 @@ assert n1 > n0, "general_dgemm_f_ did not run the split GEMM"
 size_a, size_b = (30, 7, 40), (45, 50)
 t = rng.standard_normal(30 * 7 * 40)
 m = rng.standard_normal(45 * 50)
-want = t.copy()
-oracle.special_dgemm_f_01(want, size_a, (2, 27), (5, 35), m, size_b, (10, 40), (12, 42), 1.5, 0.25)
+want = oracle.special_dgemm_f_01(t, size_a, (2, 27), (5, 35), m, size_b, (10, 40), (12, 42), 1.5, 0.25)
 got = t.copy()
 rt.special_dgemm_f_01(got, size_a, range(2, 27), 0, range(5, 35), m, size_b, range(10, 40), range(12, 42), 1.5, 0.25)
 serr = np.max(np.abs(got - want)) / np.max(np.abs(want))
