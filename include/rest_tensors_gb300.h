@@ -212,6 +212,41 @@ rt_status rt_ri_j(const double* B, const double* D, int nb, int naux, double* w,
  * float64 with a fixed-order tree.  Writes one double to ex_device. */
 rt_status rt_ri_exchange_energy(const double* D, const double* K, int nb, double* ex_device, void* stream);
 
+/* Eigen-decomposition of the symmetric n x n device matrix A (column-major;
+ * only its lower triangle is read), replacing lapack_dsyev
+ * (src/matrix/matrix_blas_lapack.rs:775-797, dsyev 'V', 'L'): eigenvalues in
+ * ascending order into w[n] (device), orthonormal eigenvectors into the
+ * columns of A.  Float64 throughout: Householder tridiagonalisation and the
+ * accumulation of its reflectors on the device, the implicit QR iteration on
+ * the tridiagonal on the host, its rotations applied on the device.  Each
+ * eigenvector's largest-magnitude component is positive.  Synchronises
+ * `stream`.  Scratch: about 3 n^2 doubles. */
+rt_status rt_dsyev(int n, double* A, double* w, void* stream);
+
+/* S^p of a symmetric n x n device matrix, replacing lapack_power
+ * (src/matrix/matrix_blas_lapack.rs:1004-1064): with S = V diag(ev) V^T,
+ *   out = sum over ev_i >= threshold of sqrt(ev_i)^p * sqrt(ev_i)^p v_i v_i^T
+ * (eigenpairs below the threshold are dropped, as the reference zeroes their
+ * columns).  n_nonsingular (host, may be NULL) receives the number kept.  The
+ * final product out = E E^T runs in the float64 form (RT_FORM_FP64) or the
+ * split form (RT_FORM_SPLIT, nslices 3..8); the eigensolver is float64.
+ * Synchronises `stream`. */
+rt_status rt_lapack_power(const double* S, int n, double p, double threshold, double* out, int* n_nonsingular,
+                          int form, int nslices, void* stream);
+
+/* The lowest num_orb eigenpairs of A x = lambda B x, replacing lapack_dspgvx
+ * (src/matrix/matrix_blas_lapack.rs:1096-1147, dspgvx itype 1, 'V', 'I', 'U'):
+ * A and B in packed upper storage (MatrixUpper: (i, j), i <= j, at
+ * ap[i + j (j + 1) / 2]) on the device, B positive definite.  eigvec[n,
+ * num_orb] receives B-orthonormal eigenvectors (x^T B x = 1), w[n] the num_orb
+ * eigenvalues in ascending order followed by zeros, as the reference's vector
+ * holds them.  Computed through B = U diag(b) U^T, X = U diag(b)^-1/2 and the
+ * eigenvectors y of X^T A X (x = X y) rather than a Cholesky factor of B; the
+ * three n x n products run in `form`.  Returns RT_ERR_INVALID_ARG when B is not
+ * positive definite (the reference panics).  Synchronises `stream`. */
+rt_status rt_dspgvx(const double* ap, const double* bp, int n, int num_orb, double* eigvec, double* w, int form,
+                    int nslices, void* stream);
+
 /* Inverse square root of a symmetric positive matrix by Newton-Schulz
  * iteration, _newton_schulz_inverse_square_root_v02
  * (src/matrix/matrix_blas_lapack.rs:1710-1778) with its per-stage iteration

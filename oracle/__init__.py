@@ -184,6 +184,36 @@ def dsyev(a, jobz="V"):
     return (a if jobz == "V" else None), w
 
 
+def lapack_power(S, p: float, threshold: float):
+    """lapack_power (matrix_blas_lapack.rs:1004-1064) through oracle.c over OpenBLAS dsyev.
+    Returns (S^p restricted to eigenvalues >= threshold, number of such eigenvalues)."""
+    S = _f(S)
+    n = S.shape[0]
+    out = np.zeros((n, n), order="F")
+    kept = ctypes.c_int(0)
+    info = lib().oracle_lapack_power(n, _p(S), ctypes.c_double(p), ctypes.c_double(threshold), _p(out),
+                                     ctypes.byref(kept))
+    if info != 0:
+        raise RuntimeError(f"dsyev info={info}")
+    return out, kept.value
+
+
+def dspgvx(ap, bp, n: int, num_orb: int):
+    """lapack_dspgvx (matrix_blas_lapack.rs:1096-1147): packed upper A and B -> (eigenvectors [n, num_orb],
+    w [n] with the num_orb eigenvalues first, m).  Raises like the reference when info != 0 or m != num_orb."""
+    ap = np.ascontiguousarray(ap, dtype=np.float64)
+    bp = np.ascontiguousarray(bp, dtype=np.float64)
+    z = np.zeros((n, num_orb), order="F")
+    w = np.zeros(n)
+    m = ctypes.c_int(0)
+    info = lib().oracle_dspgvx(n, _p(ap), _p(bp), num_orb, _p(z), _p(w), ctypes.byref(m))
+    if info != 0:
+        raise RuntimeError(f"dspgvx info={info}")
+    if m.value != num_orb:
+        raise RuntimeError(f"dspgvx returned {m.value} eigenvectors, expected {num_orb}")
+    return z, w, m.value
+
+
 def full_to_upper_packed(m) -> np.ndarray:
     """MatrixFull::to_matrixupper: column j keeps rows 0..=j (packed 'U')."""
     m = _f(m)

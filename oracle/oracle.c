@@ -36,6 +36,9 @@ typedef void (*dspevx_fn)(const char*, const char*, const char*, const int*, dou
                           int*, double*, double*, const int*, double*, int*, int*, int*);
 typedef void (*dsyev_fn)(const char*, const char*, const int*, double*, const int*, double*,
                          double*, const int*, int*);
+typedef void (*dspgvx_fn)(const int*, const char*, const char*, const char*, const int*, double*, double*,
+                          const double*, const double*, const int*, const int*, const double*, int*, double*,
+                          double*, const int*, double*, int*, int*, int*);
 typedef void (*setthreads_fn)(int);
 typedef int (*getthreads_fn)(void);
 
@@ -43,6 +46,7 @@ static dgemm_fn p_dgemm;
 static dgemv_fn p_dgemv;
 static dspevx_fn p_dspevx;
 static dsyev_fn p_dsyev;
+static dspgvx_fn p_dspgvx;
 static setthreads_fn p_set_threads;
 static getthreads_fn p_get_threads;
 
@@ -60,10 +64,11 @@ int oracle_init(const char* openblas_path) {
     p_dgemv = (dgemv_fn)sym(h, "scipy_dgemv_", "dgemv_");
     p_dspevx = (dspevx_fn)sym(h, "scipy_dspevx_", "dspevx_");
     p_dsyev = (dsyev_fn)sym(h, "scipy_dsyev_", "dsyev_");
+    p_dspgvx = (dspgvx_fn)sym(h, "scipy_dspgvx_", "dspgvx_");
     p_set_threads = (setthreads_fn)sym(h, "scipy_openblas_set_num_threads", "openblas_set_num_threads");
     p_get_threads = (getthreads_fn)sym(h, "scipy_openblas_get_num_threads", "openblas_get_num_threads");
     if (!p_dgemm || !p_dgemv) return -2;
-    if (!p_dspevx || !p_dsyev) return -3;
+    if (!p_dspevx || !p_dsyev || !p_dspgvx) return -3;
     return 0;
 }
 
@@ -253,6 +258,72 @@ int oracle_dsyev(char jobz, int n, double* a, double* w) {
     double* work = (double*)calloc((size_t)lwork + 8, sizeof(double));
     p_dsyev(&jobz, "L", &n, a, &n, w, work, &lwork, &info);
     free(work);
+    return info;
+}
+
+/*
+ * matrix_blas_lapack.rs:1004-1064 lapack_power: om = -S; dsyev('V','L') on om
+ * (:1012, through lapack_dsyev :775-797, lwork 4n); the eigenvalues negated back
+ * (largest first); columns i with ev_i >= threshold scaled by sqrt(ev_i)^p, the
+ * others zeroed (:1042-1052); out = E E^T by dgemm('N','T') (:1056-1060).
+ * n_nonsingular receives the number of eigenvalues >= threshold.  Returns the
+ * dsyev info.
+ */
+int oracle_lapack_power(int n, const double* S, double p, double threshold, double* out, int* n_nonsingular) {
+    const size_t nn = (size_t)n * (size_t)n;
+    double* om = (double*)malloc(sizeof(double) * nn + 8);
+    double* ev = (double*)malloc(sizeof(double) * (size_t)n + 8);
+    for (size_t i = 0; i < nn; ++i) om[i] = -S[i];
+    const int info = oracle_dsyev('V', n, om, ev);
+    int kept = 0;
+    for (int i = 0; i < n; ++i) {
+        ev[i] = -ev[i];
+        if (ev[i] >= threshold) ++kept;
+    }
+    for (int i = 0; i < n; ++i) {
+        double* col = om + (size_t)i * n;
+        if (i < kept) {
+            const double f = pow(sqrt(ev[i]), p);
+            for (int r = 0; r < n; ++r) col[r] *= f;
+        } else {
+            for (int r = 0; r < n; ++r) col[r] = 0.0;
+        }
+    }
+    const double one = 1.0, zero = 0.0;
+    p_dgemm("N", "T", &n, &n, &n, &one, om, &n, om, &n, &zero, out, &n);
+    if (n_nonsingular) *n_nonsingular = kept;
+    free(om); free(ev);
+    return info;
+}
+
+/*
+ * matrix_blas_lapack.rs:1096-1147 lapack_dspgvx: dspgvx(itype 1, 'V', 'I', 'U',
+ * n, a, b, vl 0, vu 0, il 1, iu num_orb, abstol SAFE_MINIMUM = 1e-16 (lib.rs:99),
+ * m, w, z, ldz n, work 8n, iwork 5n, ifail n) on packed upper copies of A and B.
+ * z receives n x num_orb eigenvectors (the reference's [ndim, num_orb] view of
+ * its n x n buffer), w all n entries (only the first m are set by LAPACK; the
+ * rest stay 0 as in the reference's zero-initialised vector).  Returns info;
+ * m_out receives m.
+ */
+int oracle_dspgvx(int n, const double* ap, const double* bp, int num_orb, double* z, double* w, int* m_out) {
+    const size_t np = (size_t)n * (size_t)(n + 1) / 2;
+    double* a = (double*)malloc(sizeof(double) * np + 8);
+    double* b = (double*)malloc(sizeof(double) * np + 8);
+    double* zz = (double*)calloc((size_t)n * (size_t)n + 8, sizeof(double));
+    double* work = (double*)calloc((size_t)8 * (size_t)n + 8, sizeof(double));
+    int* iwork = (int*)calloc((size_t)5 * (size_t)n + 8, sizeof(int));
+    int* ifail = (int*)calloc((size_t)n + 8, sizeof(int));
+    memcpy(a, ap, sizeof(double) * np);
+    memcpy(b, bp, sizeof(double) * np);
+    for (int i = 0; i < n; ++i) w[i] = 0.0;
+    const int itype = 1, il = 1, iu = num_orb, ldz = n;
+    const double vl = 0.0, vu = 0.0, abstol = 1.0e-16;
+    int m = 0, info = 0;
+    p_dspgvx(&itype, "V", "I", "U", &n, a, b, &vl, &vu, &il, &iu, &abstol, &m, w, zz, &ldz, work, iwork, ifail,
+             &info);
+    memcpy(z, zz, sizeof(double) * (size_t)n * (size_t)num_orb);
+    if (m_out) *m_out = m;
+    free(a); free(b); free(zz); free(work); free(iwork); free(ifail);
     return info;
 }
 

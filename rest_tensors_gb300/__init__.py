@@ -154,6 +154,12 @@ def lib() -> ctypes.CDLL:
     L.rt_newton_schulz_inv_sqrt.restype = c_int
     L.rt_newton_schulz_inv_sqrt.argtypes = [vp, c_int, c_dbl, c_dbl, c_int, ctypes.POINTER(c_dbl), c_int, c_int, c_int,
                                             vp, ctypes.POINTER(c_int), ctypes.POINTER(c_int), vp]
+    L.rt_dsyev.restype = c_int
+    L.rt_dsyev.argtypes = [c_int, vp, vp, vp]
+    L.rt_lapack_power.restype = c_int
+    L.rt_lapack_power.argtypes = [vp, c_int, c_dbl, c_dbl, vp, ctypes.POINTER(c_int), c_int, c_int, vp]
+    L.rt_dspgvx.restype = c_int
+    L.rt_dspgvx.argtypes = [vp, vp, c_int, c_int, vp, vp, c_int, c_int, vp]
     L.ri_ao2mo_f_.restype = None
     L.general_dgemm_f_.restype = None
     _lib = L
@@ -552,6 +558,47 @@ def newton_schulz_inverse_square_root_v02(S, n: int, threshold: float, mix_param
                                            ctypes.byref(conv),
                                            ctypes.byref(steps), _stream(stream)))
     return out, 0, bool(conv.value), int(steps.value)
+
+
+def dsyev(A, n: int, w=None, stream=None):
+    """lapack_dsyev (src/matrix/matrix_blas_lapack.rs:775-797) on a device [n, n] matrix (lower triangle read):
+    eigenvalues ascending into w (returned), eigenvectors into A's columns, in place."""
+    import torch
+
+    if w is None:
+        w = torch.empty(max(n, 1), dtype=torch.float64, device=A.device)
+    _check(lib().rt_dsyev(n, _dptr(A, n * n, "A"), _dptr(w, n, "w"), _stream(stream)))
+    return w[:n]
+
+
+def lapack_power(S, n: int, p: float, threshold: float, out=None, form: str = "fp64",
+                 nslices: int = DEFAULT_NSLICES, stream=None):
+    """lapack_power (src/matrix/matrix_blas_lapack.rs:1004-1064): S^p over the eigenvalues >= threshold.
+    Returns (out [n*n], number of eigenvalues kept)."""
+    import torch
+
+    if out is None:
+        out = torch.empty(max(n * n, 1), dtype=torch.float64, device=S.device)
+    kept = ctypes.c_int(0)
+    _check(lib().rt_lapack_power(_dptr(S, n * n, "S"), n, p, threshold, _dptr(out, n * n, "out"), ctypes.byref(kept),
+                                 _form(form), nslices, _stream(stream)))
+    return out, kept.value
+
+
+def dspgvx(ap, bp, n: int, num_orb: int, eigvec=None, w=None, form: str = "fp64", nslices: int = DEFAULT_NSLICES,
+           stream=None):
+    """lapack_dspgvx (src/matrix/matrix_blas_lapack.rs:1096-1147) on packed upper device matrices A and B:
+    the lowest num_orb eigenpairs of A x = lambda B x.  Returns (eigvec [n * num_orb], w [n])."""
+    import torch
+
+    npk = n * (n + 1) // 2
+    if eigvec is None:
+        eigvec = torch.empty(max(n * num_orb, 1), dtype=torch.float64, device=ap.device)
+    if w is None:
+        w = torch.empty(max(n, 1), dtype=torch.float64, device=ap.device)
+    _check(lib().rt_dspgvx(_dptr(ap, npk, "ap"), _dptr(bp, npk, "bp"), n, num_orb, _dptr(eigvec, n * num_orb, "eigvec"),
+                           _dptr(w, n, "w"), _form(form), nslices, _stream(stream)))
+    return eigvec, w
 
 
 def ri_j(B, D, nb: int, naux: int, w=None, J=None, stream=None):

@@ -509,139 +509,131 @@ __global__ void __launch_bounds__(256) rij_j_kernel_scalar(const double* __restr
 
 // One-pass RI-J: w_P = <B^P, D> and J = sum_P w_P B^P with one HBM read of B.
 //
-// A cooperative persistent grid of G CTAs (all co-resident); CTA c owns the
-// element range [c * chunk2, (c + 1) * chunk2) of every slab (in double2 units)
-// and keeps that part of J and of D in registers.  Slabs go in groups of S:
-//   * dot of group g: each CTA's partial <B^P, D> over its range, a fixed-order
-//     tree inside the CTA, is stored in partials[P][c]; then counts[g] += 1;
-//   * L groups later, J of group q = g - L: once counts[q] == G (a bounded wait),
-//     every CTA forms w_P = sum_c partials[P][c] in the same fixed order and adds
-//     w_P * B^P over its range, re-reading the slabs, which L2 still holds.
-// Deadlock-free because the dot of group g never waits: a CTA only waits for
-// dots of earlier groups, which every co-resident CTA reaches first.  Results
-// are bitwise reproducible (fixed reduction orders, one thread per J element).
-constexpr int RIJ1_THREADS = 512;
-constexpr int RIJ1_WARPS = RIJ1_THREADS / 32;
+// The slabs go in batches small enough that two batches stay in L2.  Launch b
+// runs two kinds of CTA side by side, none of which waits on another CTA:
+//   * dot CTAs: the partial sum <B^P, D> over one chunk of one slab of batch b,
+//     read from HBM (the lines then sit in L2);
+//   * J CTAs: for batch b-1, w_P = the fixed-order sum of that slab's chunk
+//     partials (written by launch b-1), then J += sum_P w_P B^P over one range
+//     of elements, re-reading the slabs from L2.
+// Launches after the first are programmatic dependents of their predecessor:
+// the dot CTAs (which read only B and D) start while it drains, and the J CTAs
+// wait for it to complete (griddepcontrol.wait) before reading its partials and
+// J.  Fixed reduction orders make the results bitwise reproducible.
+constexpr int RIJB_THREADS = 256;
+constexpr int RIJB_DOT_V2 = 8;  // double2 per thread of a dot CTA
+constexpr int RIJB_J_V2 = 4;    // double2 per thread of a J CTA
+constexpr int64_t RIJB_CHUNK2 = (int64_t)RIJB_THREADS * RIJB_DOT_V2;
+constexpr int64_t RIJB_JSPAN2 = (int64_t)RIJB_THREADS * RIJB_J_V2;
+constexpr int RIJB_MAX_SB = 64;
 
-struct Rij1Args {
+struct RijbArgs {
     const double2* B;  // slab P at B + P * n2h
     const double2* D;
-    int64_t n2h;       // elements of one slab / 2
-    int naux;
-    int64_t chunk2;    // double2 per CTA
-    int ngroups;
-    double* w;
     double2* J;
-    double* partials;  // [naux][G]
-    int* counts;       // [ngroups], zero on entry
-    unsigned int* err;
+    double* w;
+    double* partial;   // [naux][nchunks]
+    int64_t n2h;       // elements of one slab / 2
+    int64_t nchunks;   // dot chunks per slab
+    int naux;
+    int sb;            // slabs per batch
+    int dot_batch;     // batch this launch dots (-1: none)
+    int j_batch;       // batch this launch adds to J (-1: none)
+    int64_t dot_ctas;  // CTAs [0, dot_ctas) are dot CTAs, the rest J CTAs
+    int first_j;       // 1: J = contribution, 0: J += contribution
 };
 
-template <int S, int K2, int L>
-__global__ void __launch_bounds__(RIJ1_THREADS, 1) rij_onepass_kernel(Rij1Args a) {
-    __shared__ double red[RIJ1_WARPS][S];
-    __shared__ double ws[S];
-    __shared__ int abort_flag;
-    const int G = gridDim.x, c = blockIdx.x;
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int64_t e0 = (int64_t)c * a.chunk2;
-    const int64_t e1 = min(a.n2h, e0 + a.chunk2);
-    // This thread's elements: e0 + tid + RIJ1_THREADS * k for k < K2 (those below e1).
-    const int64_t my0 = e0 + tid;
-    const int nk = my0 < e1 ? (int)min((int64_t)K2, (e1 - my0 + RIJ1_THREADS - 1) / RIJ1_THREADS) : 0;
-    double2 d[K2], jacc[K2];
+__global__ void __launch_bounds__(RIJB_THREADS) rij_batch_kernel(RijbArgs a) {
+    __shared__ double red[RIJB_THREADS / 32];
+    __shared__ double ws[RIJB_MAX_SB];
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if ((int64_t)blockIdx.x < a.dot_ctas) {
+        const int64_t item = blockIdx.x;
+        const int P = a.dot_batch * a.sb + (int)(item / a.nchunks);
+        const int64_t c = item % a.nchunks;
+        const double2* b = a.B + (int64_t)P * a.n2h;
+        const int64_t e0 = c * RIJB_CHUNK2 + tid;
+        double2 x[RIJB_DOT_V2], y[RIJB_DOT_V2];
 #pragma unroll
-    for (int k = 0; k < K2; ++k) {
-        d[k] = k < nk ? a.D[my0 + (int64_t)RIJ1_THREADS * k] : make_double2(0.0, 0.0);
-        jacc[k] = make_double2(0.0, 0.0);
+        for (int u = 0; u < RIJB_DOT_V2; ++u) {
+            const int64_t idx = e0 + (int64_t)RIJB_THREADS * u;
+            x[u] = idx < a.n2h ? b[idx] : make_double2(0.0, 0.0);
+            y[u] = idx < a.n2h ? a.D[idx] : make_double2(0.0, 0.0);
+        }
+        double s0 = 0.0, s1 = 0.0;
+#pragma unroll
+        for (int u = 0; u < RIJB_DOT_V2; u += 2) {
+            s0 = fma(x[u].y, y[u].y, fma(x[u].x, y[u].x, s0));
+            s1 = fma(x[u + 1].y, y[u + 1].y, fma(x[u + 1].x, y[u + 1].x, s1));
+        }
+        double t = s0 + s1;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (lane == 0) red[warp] = t;
+        __syncthreads();
+        if (warp == 0) {
+            double r = lane < RIJB_THREADS / 32 ? red[lane] : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+            if (lane == 0) a.partial[(int64_t)P * a.nchunks + c] = r;
+        }
+        return;
     }
-    if (tid == 0) abort_flag = 0;
+    // J CTA: wait until the previous launch (its dots of this batch, its J) is complete.
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    const int P0 = a.j_batch * a.sb;
+    const int np = min(a.sb, a.naux - P0);
+    for (int s = warp; s < np; s += RIJB_THREADS / 32) {
+        double t = 0.0;
+        for (int64_t c = lane; c < a.nchunks; c += 32) t += a.partial[(int64_t)(P0 + s) * a.nchunks + c];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (lane == 0) ws[s] = t;
+    }
     __syncthreads();
-    for (int g = 0; g < a.ngroups + L; ++g) {
-        if (g < a.ngroups) {
-            const int P0 = g * S;
-            double2 x[S][K2];
+    if ((int64_t)blockIdx.x == a.dot_ctas && tid < np && a.w) a.w[P0 + tid] = ws[tid];
+    const int64_t e0 = ((int64_t)blockIdx.x - a.dot_ctas) * RIJB_JSPAN2 + tid;
+    double2 acc[RIJB_J_V2];
 #pragma unroll
-            for (int s = 0; s < S; ++s)
+    for (int u = 0; u < RIJB_J_V2; ++u) {
+        const int64_t idx = e0 + (int64_t)RIJB_THREADS * u;
+        acc[u] = (!a.first_j && idx < a.n2h) ? a.J[idx] : make_double2(0.0, 0.0);
+    }
+    int s = 0;
+    for (; s + 2 <= np; s += 2) {  // two slabs' loads in flight, added in slab order
+        const double w0 = ws[s], w1 = ws[s + 1];
+        const double2* b0 = a.B + (int64_t)(P0 + s) * a.n2h;
+        const double2* b1 = b0 + a.n2h;
+        double2 x0[RIJB_J_V2], x1[RIJB_J_V2];
 #pragma unroll
-                for (int k = 0; k < K2; ++k)
-                    x[s][k] = (P0 + s < a.naux && k < nk)
-                                  ? a.B[(int64_t)(P0 + s) * a.n2h + my0 + (int64_t)RIJ1_THREADS * k]
-                                  : make_double2(0.0, 0.0);
-            double acc[S];
-#pragma unroll
-            for (int s = 0; s < S; ++s) {
-                acc[s] = 0.0;
-#pragma unroll
-                for (int k = 0; k < K2; ++k) acc[s] = fma(x[s][k].y, d[k].y, fma(x[s][k].x, d[k].x, acc[s]));
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) acc[s] += __shfl_xor_sync(0xffffffffu, acc[s], o);
-            }
-            if (lane == 0) {
-#pragma unroll
-                for (int s = 0; s < S; ++s) red[warp][s] = acc[s];
-            }
-            __syncthreads();
-            if (tid < S && P0 + tid < a.naux) {
-                double t = 0.0;
-#pragma unroll
-                for (int w = 0; w < RIJ1_WARPS; ++w) t += red[w][tid];
-                a.partials[(int64_t)(P0 + tid) * G + c] = t;
-                __threadfence();
-            }
-            __syncthreads();
-            if (tid == 0) atomicAdd(&a.counts[g], 1);
+        for (int u = 0; u < RIJB_J_V2; ++u) {
+            const int64_t idx = e0 + (int64_t)RIJB_THREADS * u;
+            x0[u] = idx < a.n2h ? b0[idx] : make_double2(0.0, 0.0);
+            x1[u] = idx < a.n2h ? b1[idx] : make_double2(0.0, 0.0);
         }
-        if (g >= L) {
-            const int q = g - L, Q0 = q * S;
-            if (tid == 0) {
-                volatile int* cnt = a.counts + q;
-                if (*cnt < G) {
-                    const long long t0 = clock64();
-                    while (*cnt < G) {
-                        if (clock64() - t0 > ptx::kWaitCycles) {
-                            atomicOr(a.err, DEV_ERR_TIMEOUT);
-                            abort_flag = 1;
-                            break;
-                        }
-                    }
-                }
-                __threadfence();
-            }
-            __syncthreads();
-            if (abort_flag) return;
-            if (warp < S) {
-                double t = 0.0;
-                if (Q0 + warp < a.naux)
-                    for (int cc = lane; cc < G; cc += 32) t += __ldcg(a.partials + (int64_t)(Q0 + warp) * G + cc);
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-                if (lane == 0) ws[warp] = t;
-            }
-            __syncthreads();
-            if (c == 0 && tid < S && Q0 + tid < a.naux && a.w) a.w[Q0 + tid] = ws[tid];
-            double2 y[S][K2];
+        for (int u = 0; u < RIJB_J_V2; ++u) {
+            acc[u].x = fma(w1, x1[u].x, fma(w0, x0[u].x, acc[u].x));
+            acc[u].y = fma(w1, x1[u].y, fma(w0, x0[u].y, acc[u].y));
+        }
+    }
+    if (s < np) {
+        const double w0 = ws[s];
+        const double2* b0 = a.B + (int64_t)(P0 + s) * a.n2h;
 #pragma unroll
-            for (int s = 0; s < S; ++s)
-#pragma unroll
-                for (int k = 0; k < K2; ++k)
-                    y[s][k] = (Q0 + s < a.naux && k < nk)
-                                  ? a.B[(int64_t)(Q0 + s) * a.n2h + my0 + (int64_t)RIJ1_THREADS * k]
-                                  : make_double2(0.0, 0.0);
-#pragma unroll
-            for (int s = 0; s < S; ++s) {
-                const double wv = ws[s];
-#pragma unroll
-                for (int k = 0; k < K2; ++k) {
-                    jacc[k].x = fma(wv, y[s][k].x, jacc[k].x);
-                    jacc[k].y = fma(wv, y[s][k].y, jacc[k].y);
-                }
-            }
+        for (int u = 0; u < RIJB_J_V2; ++u) {
+            const int64_t idx = e0 + (int64_t)RIJB_THREADS * u;
+            const double2 x0 = idx < a.n2h ? b0[idx] : make_double2(0.0, 0.0);
+            acc[u].x = fma(w0, x0.x, acc[u].x);
+            acc[u].y = fma(w0, x0.y, acc[u].y);
         }
     }
 #pragma unroll
-    for (int k = 0; k < K2; ++k)
-        if (k < nk) a.J[my0 + (int64_t)RIJ1_THREADS * k] = jacc[k];
+    for (int u = 0; u < RIJB_J_V2; ++u) {
+        const int64_t idx = e0 + (int64_t)RIJB_THREADS * u;
+        if (idx < a.n2h) a.J[idx] = acc[u];
+    }
 }
 
 // -tr(D K) with one CTA and a fixed reduction tree (bitwise reproducible).
@@ -684,89 +676,51 @@ __global__ void synth_kernel(uint64_t seed, int nb, int P0, int64_t total, doubl
 
 }  // namespace
 
-template <int S, int K2>
-cudaError_t launch_rij1(const Rij1Args& a, int G, cudaStream_t stream) {
-    void* args[] = {const_cast<Rij1Args*>(&a)};
-    return cudaLaunchCooperativeKernel((const void*)rij_onepass_kernel<S, K2, 1>, dim3((unsigned)G),
-                                       dim3(RIJ1_THREADS), args, 0, stream);
-}
-
-// S slabs per group for K2 double2 per thread and slab, S * K2 <= 16.
-template <int K2>
-cudaError_t launch_rij1_s(const Rij1Args& a, int S, int G, cudaStream_t stream) {
-    if constexpr (8 * K2 <= 16) {
-        if (S >= 8) return launch_rij1<8, K2>(a, G, stream);
-    }
-    if constexpr (4 * K2 <= 16) {
-        if (S >= 4) return launch_rij1<4, K2>(a, G, stream);
-    }
-    if constexpr (2 * K2 <= 16) {
-        if (S >= 2) return launch_rij1<2, K2>(a, G, stream);
-    }
-    return launch_rij1<1, K2>(a, G, stream);
-}
-
-// The one-pass form when the layout suits it (even slab length, 16-byte aligned
-// slabs, at most 16 double2 per thread and slab); `done` tells the caller
-// whether it ran.  Slabs per group: at most 8, two groups within ~48 MB so the
-// re-read of the lagging group still hits L2, and at most 16 double2 of slab
-// data per thread and group (no register spills at 512 threads).
+// The one-pass form when the layout suits it (even slab length, 16-byte
+// aligned B, D and J); `done` tells the caller whether it ran.  Slabs per batch:
+// about 40 MB, so that the batch being added to J and the one being dotted fit
+// in L2 together.
 rt_status ri_j_onepass(const double* B, const double* D, int64_t n2, int naux, double* w, double* J,
                        cudaStream_t stream, bool& done) {
     done = false;
     if ((n2 & 1) || ((uintptr_t)B & 15) || ((uintptr_t)D & 15) || ((uintptr_t)J & 15) || naux <= 0) return RT_OK;
-    const int64_t n2h = n2 / 2;
-    const int G = (int)std::max<int64_t>(1, std::min<int64_t>(sm_count(), ceil_div(n2h, RIJ1_THREADS)));
-    const int64_t chunk2 = ceil_div(n2h, G);
-    const int64_t need = ceil_div(chunk2, RIJ1_THREADS);
-    static const int kK2[] = {1, 2, 3, 4, 6, 8, 12, 16};
-    int K2 = 0;
-    for (int k : kK2)
-        if (!K2 && k >= need) K2 = k;
-    if (!K2) return RT_OK;
-    const int64_t slab_bytes = 16 * n2h;
-    int64_t smax = std::min<int64_t>({8, std::max<int64_t>(1, ((int64_t)24 << 20) / slab_bytes), 16 / K2});
-    int S = 1;
-    while (S * 2 <= smax) S *= 2;
-    const int ngroups = (int)ceil_div(naux, S);
-    ScratchBuf sb;
-    const size_t pbytes = align_up(sizeof(double) * (size_t)naux * G, 256);
-    RT_TRY(scratch_alloc(sb, pbytes + sizeof(int) * (size_t)ngroups, stream));
-    int* counts = reinterpret_cast<int*>(sb.as<uint8_t>() + pbytes);
-    RT_CUDA_TRY(cudaMemsetAsync(counts, 0, sizeof(int) * (size_t)ngroups, stream));
-    unsigned int* err = error_word_device();
-    RT_REQUIRE(err != nullptr, "ri_j: device error word unavailable");
-    Rij1Args a;
+    RijbArgs a;
     a.B = reinterpret_cast<const double2*>(B);
     a.D = reinterpret_cast<const double2*>(D);
-    a.n2h = n2h;
-    a.naux = naux;
-    a.chunk2 = chunk2;
-    a.ngroups = ngroups;
-    a.w = w;
     a.J = reinterpret_cast<double2*>(J);
-    a.partials = sb.as<double>();
-    a.counts = counts;
-    a.err = err;
+    a.w = w;
+    a.n2h = n2 / 2;
+    a.nchunks = ceil_div(a.n2h, RIJB_CHUNK2);
+    a.naux = naux;
+    a.sb = (int)std::max<int64_t>(1, std::min<int64_t>({RIJB_MAX_SB, (int64_t)naux,
+                                                        ((int64_t)40 << 20) / std::max<int64_t>(16 * a.n2h, 1)}));
+    const int nbatch = (int)ceil_div(naux, a.sb);
+    ScratchBuf pb;
+    RT_TRY(scratch_alloc(pb, sizeof(double) * (size_t)naux * (size_t)a.nchunks, stream));
+    a.partial = pb.as<double>();
+    const int64_t jctas = ceil_div(a.n2h, RIJB_JSPAN2);
     prof_begin(PROF_RIJ, stream);
-    cudaError_t e;
-    switch (K2) {
-        case 1: e = launch_rij1_s<1>(a, S, G, stream); break;
-        case 2: e = launch_rij1_s<2>(a, S, G, stream); break;
-        case 3: e = launch_rij1_s<3>(a, S, G, stream); break;
-        case 4: e = launch_rij1_s<4>(a, S, G, stream); break;
-        case 6: e = launch_rij1_s<6>(a, S, G, stream); break;
-        case 8: e = launch_rij1_s<8>(a, S, G, stream); break;
-        case 12: e = launch_rij1_s<12>(a, S, G, stream); break;
-        default: e = launch_rij1_s<16>(a, S, G, stream); break;
+    for (int b = 0; b <= nbatch; ++b) {
+        a.dot_batch = b < nbatch ? b : -1;
+        a.j_batch = b >= 1 ? b - 1 : -1;
+        a.dot_ctas = b < nbatch ? (int64_t)std::min(a.sb, naux - b * a.sb) * a.nchunks : 0;
+        a.first_j = b == 1 ? 1 : 0;
+        const int64_t grid = a.dot_ctas + (b >= 1 ? jctas : 0);
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)grid);
+        cfg.blockDim = dim3(RIJB_THREADS);
+        cfg.dynamicSmemBytes = 0;
+        cfg.stream = stream;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        // The first launch is an ordinary one: whatever wrote B and D before it completes first.
+        cfg.attrs = b >= 1 ? attr : nullptr;
+        cfg.numAttrs = b >= 1 ? 1 : 0;
+        RT_CUDA_TRY(cudaLaunchKernelEx(&cfg, rij_batch_kernel, a));
+        RT_TRY(check_launch("rij_batch_kernel"));
     }
-    if (e == cudaErrorCooperativeLaunchTooLarge || e == cudaErrorNotSupported) {
-        cudaGetLastError();  // not co-residable here: the two-pass kernels run instead
-        return RT_OK;
-    }
-    RT_CUDA_TRY(e);
-    prof_end(PROF_RIJ, stream, 16.0 * (double)n2h * naux);
-    RT_TRY(check_launch("rij_onepass_kernel"));
+    prof_end(PROF_RIJ, stream, 8.0 * (double)n2 * naux);
     done = true;
     return RT_OK;
 }

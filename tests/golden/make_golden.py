@@ -86,6 +86,30 @@ def extract(ref: str) -> dict:
         "eigvec": _floats(vec_txt.split("vec!")[1]), "eigval": _floats(L[k].split("vec!")[1]),
     })
 
+    # lapack_power test inputs (the tests print their results without asserting): the
+    # 3x3 SPD matrix of test_sqrt_inverse and the 8x8 matrix of matfull_inverse_and_power.
+    num = r"(-?\d+(?:\.\d+)?(?:[eE]-?\d+)?)"
+    i = _line_of(L, r"fn test_sqrt_inverse")
+    j = _line_of(L, r"lapack_power\(", i)
+    vec_txt = " ".join(L[i:j])
+    pm = re.search(r"lapack_power\(" + num + r",\s*" + num + r"\)", L[j])
+    out["cases"].append({
+        "name": "lapack_power_3x3", "where": f"src/matrix/matrix_blas_lapack.rs:{i + 1}-{j + 1}",
+        "n": 3, "matrix": _floats(vec_txt.split("vec!")[1]), "p": float(pm.group(1)),
+        "threshold": float(pm.group(2)),
+    })
+    p = os.path.join(ref, "src/lib.rs")
+    L = open(p).read().splitlines()
+    i = _line_of(L, r"fn matfull_inverse_and_power")
+    k = _line_of(L, r"let orig_a = vec!\[", i)
+    j = _line_of(L, r"lapack_power\(", k)
+    pm = re.search(r"lapack_power\(" + num + r",\s*" + num + r"\)", L[j])
+    mat = _floats(L[k].split("vec!")[1])
+    out["cases"].append({
+        "name": "lapack_power_8x8", "where": f"src/lib.rs:{k + 1}-{j + 1}",
+        "n": int(round(len(mat) ** 0.5)), "matrix": mat, "p": float(pm.group(1)), "threshold": float(pm.group(2)),
+    })
+
     # criterion bench input: RIFull [10,10,20] filled with 2.0, eigenvector ones(10,10)
     p = os.path.join(ref, "benches/bench_tensors.rs")
     L = open(p).read().splitlines()
