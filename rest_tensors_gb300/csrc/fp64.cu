@@ -11,7 +11,6 @@
 #include <mutex>
 
 #include "rt_internal.cuh"
-#include "rt_ptx.cuh"
 #include "../../include/rt_synth.h"
 
 namespace rt {
@@ -507,135 +506,6 @@ __global__ void __launch_bounds__(256) rij_j_kernel_scalar(const double* __restr
     J[e] = a0 + a1;
 }
 
-// One-pass RI-J: w_P = <B^P, D> and J = sum_P w_P B^P with one HBM read of B.
-//
-// The slabs go in batches small enough that two batches stay in L2.  Launch b
-// runs two kinds of CTA side by side, none of which waits on another CTA:
-//   * dot CTAs: the partial sum <B^P, D> over one chunk of one slab of batch b,
-//     read from HBM (the lines then sit in L2);
-//   * J CTAs: for batch b-1, w_P = the fixed-order sum of that slab's chunk
-//     partials (written by launch b-1), then J += sum_P w_P B^P over one range
-//     of elements, re-reading the slabs from L2.
-// Launches after the first are programmatic dependents of their predecessor:
-// the dot CTAs (which read only B and D) start while it drains, and the J CTAs
-// wait for it to complete (griddepcontrol.wait) before reading its partials and
-// J.  Fixed reduction orders make the results bitwise reproducible.
-constexpr int RIJB_THREADS = 256;
-constexpr int RIJB_DOT_V2 = 8;  // double2 per thread of a dot CTA
-constexpr int RIJB_J_V2 = 4;    // double2 per thread of a J CTA
-constexpr int64_t RIJB_CHUNK2 = (int64_t)RIJB_THREADS * RIJB_DOT_V2;
-constexpr int64_t RIJB_JSPAN2 = (int64_t)RIJB_THREADS * RIJB_J_V2;
-constexpr int RIJB_MAX_SB = 64;
-
-struct RijbArgs {
-    const double2* B;  // slab P at B + P * n2h
-    const double2* D;
-    double2* J;
-    double* w;
-    double* partial;   // [naux][nchunks]
-    int64_t n2h;       // elements of one slab / 2
-    int64_t nchunks;   // dot chunks per slab
-    int naux;
-    int sb;            // slabs per batch
-    int dot_batch;     // batch this launch dots (-1: none)
-    int j_batch;       // batch this launch adds to J (-1: none)
-    int64_t dot_ctas;  // CTAs [0, dot_ctas) are dot CTAs, the rest J CTAs
-    int first_j;       // 1: J = contribution, 0: J += contribution
-};
-
-__global__ void __launch_bounds__(RIJB_THREADS) rij_batch_kernel(RijbArgs a) {
-    __shared__ double red[RIJB_THREADS / 32];
-    __shared__ double ws[RIJB_MAX_SB];
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if ((int64_t)blockIdx.x < a.dot_ctas) {
-        const int64_t item = blockIdx.x;
-        const int P = a.dot_batch * a.sb + (int)(item / a.nchunks);
-        const int64_t c = item % a.nchunks;
-        const double2* b = a.B + (int64_t)P * a.n2h;
-        const int64_t e0 = c * RIJB_CHUNK2 + tid;
-        double2 x[RIJB_DOT_V2], y[RIJB_DOT_V2];
-#pragma unroll
-        for (int u = 0; u < RIJB_DOT_V2; ++u) {
-            const int64_t idx = e0 + (int64_t)RIJB_THREADS * u;
-            x[u] = idx < a.n2h ? b[idx] : make_double2(0.0, 0.0);
-            y[u] = idx < a.n2h ? a.D[idx] : make_double2(0.0, 0.0);
-        }
-        double s0 = 0.0, s1 = 0.0;
-#pragma unroll
-        for (int u = 0; u < RIJB_DOT_V2; u += 2) {
-            s0 = fma(x[u].y, y[u].y, fma(x[u].x, y[u].x, s0));
-            s1 = fma(x[u + 1].y, y[u + 1].y, fma(x[u + 1].x, y[u + 1].x, s1));
-        }
-        double t = s0 + s1;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-        if (lane == 0) red[warp] = t;
-        __syncthreads();
-        if (warp == 0) {
-            double r = lane < RIJB_THREADS / 32 ? red[lane] : 0.0;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
-            if (lane == 0) a.partial[(int64_t)P * a.nchunks + c] = r;
-        }
-        return;
-    }
-    // J CTA: wait until the previous launch (its dots of this batch, its J) is complete.
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-    const int P0 = a.j_batch * a.sb;
-    const int np = min(a.sb, a.naux - P0);
-    for (int s = warp; s < np; s += RIJB_THREADS / 32) {
-        double t = 0.0;
-        for (int64_t c = lane; c < a.nchunks; c += 32) t += a.partial[(int64_t)(P0 + s) * a.nchunks + c];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-        if (lane == 0) ws[s] = t;
-    }
-    __syncthreads();
-    if ((int64_t)blockIdx.x == a.dot_ctas && tid < np && a.w) a.w[P0 + tid] = ws[tid];
-    const int64_t e0 = ((int64_t)blockIdx.x - a.dot_ctas) * RIJB_JSPAN2 + tid;
-    double2 acc[RIJB_J_V2];
-#pragma unroll
-    for (int u = 0; u < RIJB_J_V2; ++u) {
-        const int64_t idx = e0 + (int64_t)RIJB_THREADS * u;
-        acc[u] = (!a.first_j && idx < a.n2h) ? a.J[idx] : make_double2(0.0, 0.0);
-    }
-    int s = 0;
-    for (; s + 2 <= np; s += 2) {  // two slabs' loads in flight, added in slab order
-        const double w0 = ws[s], w1 = ws[s + 1];
-        const double2* b0 = a.B + (int64_t)(P0 + s) * a.n2h;
-        const double2* b1 = b0 + a.n2h;
-        double2 x0[RIJB_J_V2], x1[RIJB_J_V2];
-#pragma unroll
-        for (int u = 0; u < RIJB_J_V2; ++u) {
-            const int64_t idx = e0 + (int64_t)RIJB_THREADS * u;
-            x0[u] = idx < a.n2h ? b0[idx] : make_double2(0.0, 0.0);
-            x1[u] = idx < a.n2h ? b1[idx] : make_double2(0.0, 0.0);
-        }
-#pragma unroll
-        for (int u = 0; u < RIJB_J_V2; ++u) {
-            acc[u].x = fma(w1, x1[u].x, fma(w0, x0[u].x, acc[u].x));
-            acc[u].y = fma(w1, x1[u].y, fma(w0, x0[u].y, acc[u].y));
-        }
-    }
-    if (s < np) {
-        const double w0 = ws[s];
-        const double2* b0 = a.B + (int64_t)(P0 + s) * a.n2h;
-#pragma unroll
-        for (int u = 0; u < RIJB_J_V2; ++u) {
-            const int64_t idx = e0 + (int64_t)RIJB_THREADS * u;
-            const double2 x0 = idx < a.n2h ? b0[idx] : make_double2(0.0, 0.0);
-            acc[u].x = fma(w0, x0.x, acc[u].x);
-            acc[u].y = fma(w0, x0.y, acc[u].y);
-        }
-    }
-#pragma unroll
-    for (int u = 0; u < RIJB_J_V2; ++u) {
-        const int64_t idx = e0 + (int64_t)RIJB_THREADS * u;
-        if (idx < a.n2h) a.J[idx] = acc[u];
-    }
-}
-
 // -tr(D K) with one CTA and a fixed reduction tree (bitwise reproducible).
 __global__ void __launch_bounds__(1024) exchange_kernel(const double* __restrict__ D, const double* __restrict__ K,
                                                         int64_t n2, double* __restrict__ out) {
@@ -676,55 +546,6 @@ __global__ void synth_kernel(uint64_t seed, int nb, int P0, int64_t total, doubl
 
 }  // namespace
 
-// The one-pass form when the layout suits it (even slab length, 16-byte
-// aligned B, D and J); `done` tells the caller whether it ran.  Slabs per batch:
-// about 40 MB, so that the batch being added to J and the one being dotted fit
-// in L2 together.
-rt_status ri_j_onepass(const double* B, const double* D, int64_t n2, int naux, double* w, double* J,
-                       cudaStream_t stream, bool& done) {
-    done = false;
-    if ((n2 & 1) || ((uintptr_t)B & 15) || ((uintptr_t)D & 15) || ((uintptr_t)J & 15) || naux <= 0) return RT_OK;
-    RijbArgs a;
-    a.B = reinterpret_cast<const double2*>(B);
-    a.D = reinterpret_cast<const double2*>(D);
-    a.J = reinterpret_cast<double2*>(J);
-    a.w = w;
-    a.n2h = n2 / 2;
-    a.nchunks = ceil_div(a.n2h, RIJB_CHUNK2);
-    a.naux = naux;
-    a.sb = (int)std::max<int64_t>(1, std::min<int64_t>({RIJB_MAX_SB, (int64_t)naux,
-                                                        ((int64_t)40 << 20) / std::max<int64_t>(16 * a.n2h, 1)}));
-    const int nbatch = (int)ceil_div(naux, a.sb);
-    ScratchBuf pb;
-    RT_TRY(scratch_alloc(pb, sizeof(double) * (size_t)naux * (size_t)a.nchunks, stream));
-    a.partial = pb.as<double>();
-    const int64_t jctas = ceil_div(a.n2h, RIJB_JSPAN2);
-    prof_begin(PROF_RIJ, stream);
-    for (int b = 0; b <= nbatch; ++b) {
-        a.dot_batch = b < nbatch ? b : -1;
-        a.j_batch = b >= 1 ? b - 1 : -1;
-        a.dot_ctas = b < nbatch ? (int64_t)std::min(a.sb, naux - b * a.sb) * a.nchunks : 0;
-        a.first_j = b == 1 ? 1 : 0;
-        const int64_t grid = a.dot_ctas + (b >= 1 ? jctas : 0);
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3((unsigned)grid);
-        cfg.blockDim = dim3(RIJB_THREADS);
-        cfg.dynamicSmemBytes = 0;
-        cfg.stream = stream;
-        cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-        attr[0].val.programmaticStreamSerializationAllowed = 1;
-        // The first launch is an ordinary one: whatever wrote B and D before it completes first.
-        cfg.attrs = b >= 1 ? attr : nullptr;
-        cfg.numAttrs = b >= 1 ? 1 : 0;
-        RT_CUDA_TRY(cudaLaunchKernelEx(&cfg, rij_batch_kernel, a));
-        RT_TRY(check_launch("rij_batch_kernel"));
-    }
-    prof_end(PROF_RIJ, stream, 8.0 * (double)n2 * naux);
-    done = true;
-    return RT_OK;
-}
-
 rt_status ri_j_fp64(const double* B, const double* D, int nb, int naux, double* w, double* J,
                     cudaStream_t stream) {
     const int64_t n2 = (int64_t)nb * nb;
@@ -732,11 +553,6 @@ rt_status ri_j_fp64(const double* B, const double* D, int nb, int naux, double* 
     if (!w) {
         RT_TRY(scratch_alloc(wbuf, sizeof(double) * (size_t)naux, stream));
         w = wbuf.as<double>();
-    }
-    if (J) {
-        bool done = false;
-        RT_TRY(ri_j_onepass(B, D, n2, naux, w, J, stream, done));
-        if (done) return RT_OK;
     }
     rij_w_kernel<<<(unsigned)naux, 256, 0, stream>>>(B, D, n2, naux, w);
     RT_TRY(check_launch("rij_w_kernel"));

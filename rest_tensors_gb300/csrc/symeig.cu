@@ -17,8 +17,8 @@
 //  3. The implicit symmetric QR iteration with Wilkinson shifts on (d, e)
 //     (Algorithm 8.3.3) on the host: O(n) per sweep; its Givens rotations are
 //     recorded and
-//  4. applied to the rows of Q on the device (one thread per row, the sweep's
-//     rotations in order, the shared column carried in a register).
+//  4. applied to the rows of Q on the device, 32 sweeps per pass in a systolic
+//     warp per row (lane j applies sweep j, columns passed lane to lane).
 //  5. Eigenvalues sorted ascending; each eigenvector's largest-magnitude
 //     component made positive (LAPACK fixes no sign either).
 // All reductions have a fixed order, so results are bitwise reproducible.
@@ -192,39 +192,76 @@ __global__ void lower_to_full_kernel(const double* __restrict__ in, double* __re
 
 // Recorded Givens sweeps of the QR iteration: sweep s rotates columns
 // (k, k+1) for k = lo[s] .. hi[s]-1 with (c, s) at rot[first[s] + k - lo[s]]:
-//   z_k <- c z_k + s z_{k+1},   z_{k+1} <- -s z_k + c z_{k+1}.
-// One thread per row of Z; the column shared by consecutive rotations is
-// carried in a register.
-__global__ void __launch_bounds__(128) apply_rotations_kernel(double* __restrict__ Z, int64_t n,
-                                                              const int* __restrict__ lo, const int* __restrict__ hi,
-                                                              const int64_t* __restrict__ first,
-                                                              const double2* __restrict__ rot, int nsweeps) {
-    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= n) return;
-    double* z = Z + r;
-    for (int sw = 0; sw < nsweeps; ++sw) {
-        const int l = __ldg(lo + sw), h = __ldg(hi + sw);
-        const double2* R = rot + __ldg(first + sw) - l;
-        double carry = z[(int64_t)l * n];
-        int k = l;
-        for (; k + 4 <= h; k += 4) {
-            double nx[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) nx[u] = z[(int64_t)(k + u + 1) * n];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const double2 cs = __ldg(R + k + u);
-                z[(int64_t)(k + u) * n] = fma(cs.x, carry, cs.y * nx[u]);
-                carry = fma(cs.x, nx[u], -cs.y * carry);
-            }
+//   z_k <- c z_k + s z_{k+1},   z_{k+1} <- -s z_k + c z_{k+1},
+// applied to every row of Z.
+//
+// Systolic form: 32 consecutive sweeps per pass, one warp per row, lane j
+// applying sweep s0 + j.  At step t lane j rotates columns (t - 2j, t - 2j + 1):
+// it holds column t - 2j, receives column t - 2j + 1 from lane j - 1 (which
+// finished it in step t - 1) and hands the finished column t - 2j to lane j + 1.
+// Lane 0 takes the row's next column, lane 31 returns column t - 62, which every
+// sweep of the pass has finished.  The order of the rotations on each column
+// pair is that of the sweeps, so the result is the sequential one.  Columns pass
+// through shared-memory tiles of 32 columns x ROWS rows (coalesced loads and
+// stores), and each 32-step chunk's rotations are staged in shared memory, an
+// identity where a sweep has no rotation, so the steps have no branches.  The
+// FP64 work is spread over 32 lanes per row.
+constexpr int kSysRows = 16;
+
+__global__ void __launch_bounds__(kSysRows * 32) rot_systolic_kernel(double* __restrict__ Z, int64_t n,
+                                                                     const int* __restrict__ lo,
+                                                                     const int* __restrict__ hi,
+                                                                     const int64_t* __restrict__ first,
+                                                                     const double2* __restrict__ rot, int s0,
+                                                                     int nsw) {
+    __shared__ double tin[kSysRows][33];
+    __shared__ double tout[kSysRows][33];
+    __shared__ double2 prm[32][33];
+    __shared__ int slo[32], shi[32];
+    __shared__ int64_t sfirst[32];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (tid < 32) {
+        const bool on = tid < nsw;
+        slo[tid] = on ? lo[s0 + tid] : 1 << 30;
+        shi[tid] = on ? hi[s0 + tid] : -1;
+        sfirst[tid] = on ? first[s0 + tid] : 0;
+    }
+    __syncthreads();
+    int cmin = 1 << 30, cmax = -1;
+    for (int j = 0; j < nsw; ++j) {
+        cmin = min(cmin, slo[j]);
+        cmax = max(cmax, shi[j]);
+    }
+    const int64_t row0 = (int64_t)blockIdx.x * kSysRows;
+    double lower = 0.0, out = 0.0;
+    // tile element (row w', column offset i) is moved by thread (w' + kSysRows * i) % blockDim
+    const int mw = tid % kSysRows, mi = tid / kSysRows;  // mi in 0..31
+    const bool mrow = row0 + mw < n;
+    for (int T = cmin - 1; T <= cmax + 62; T += 32) {
+        {
+            const int c = T + 1 + mi;
+            tin[mw][mi] = (mrow && c >= cmin && c <= cmax) ? Z[row0 + mw + (int64_t)c * n] : 0.0;
         }
-        for (; k < h; ++k) {
-            const double nx = z[(int64_t)(k + 1) * n];
-            const double2 cs = __ldg(R + k);
-            z[(int64_t)k * n] = fma(cs.x, carry, cs.y * nx);
-            carry = fma(cs.x, nx, -cs.y * carry);
+        for (int q = tid; q < 32 * 32; q += kSysRows * 32) {
+            const int j = q >> 5, u = q & 31;
+            const int k = T + u - 2 * j;
+            prm[j][u] = (k >= slo[j] && k < shi[j]) ? rot[sfirst[j] + (k - slo[j])] : make_double2(1.0, 0.0);
         }
-        z[(int64_t)h * n] = carry;
+        __syncthreads();
+#pragma unroll 8
+        for (int u = 0; u < 32; ++u) {
+            double upper = __shfl_up_sync(0xffffffffu, out, 1);
+            if (lane == 0) upper = tin[w][u];
+            const double2 cs = prm[lane][u];
+            out = fma(cs.x, lower, cs.y * upper);
+            lower = fma(cs.x, upper, -cs.y * lower);
+            if (lane == 31) tout[w][u] = out;
+        }
+        __syncthreads();
+        {
+            const int c = T - 62 + mi;
+            if (mrow && c >= cmin && c <= cmax) Z[row0 + mw + (int64_t)c * n] = tout[mw][mi];
+        }
     }
 }
 
@@ -255,15 +292,23 @@ __global__ void __launch_bounds__(256) sort_sign_kernel(const double* __restrict
 
 // Implicit symmetric QR with Wilkinson shifts on the tridiagonal (d, e),
 // recording every sweep's rotations.  Returns false without convergence in 30 n
-// sweeps.  Rotations follow the convention of apply_rotations_kernel.
+// sweeps.  Rotations follow the convention of rot_systolic_kernel.
 struct Sweeps {
     std::vector<int> lo, hi;
     std::vector<int64_t> first;
     std::vector<double2> rot;
 };
 
+// sqrt(x^2 + y^2), through hypot only where the squares could overflow or underflow.
+inline double norm2(double x, double y) {
+    const double ax = fabs(x), ay = fabs(y), m = ax > ay ? ax : ay;
+    if (m < 1e150 && (m > 1e-150 || m == 0.0)) return sqrt(x * x + y * y);
+    return hypot(x, y);
+}
+
 bool tridiag_qr(int n, std::vector<double>& d, std::vector<double>& e, Sweeps& sw) {
     const double eps = 2.220446049250313e-16;
+    sw.rot.reserve((size_t)n * (size_t)n);
     int hi = n - 1, steps = 0;
     while (hi > 0) {
         if (fabs(e[hi - 1]) <= eps * (fabs(d[hi - 1]) + fabs(d[hi]))) {
@@ -285,7 +330,7 @@ bool tridiag_qr(int n, std::vector<double>& d, std::vector<double>& e, Sweeps& s
         sw.first.push_back((int64_t)sw.rot.size());
         for (int k = lo; k < hi; ++k) {
             // [c s; -s c] on rows/columns k, k+1 maps (x, bulge) to (r, 0).
-            const double r = hypot(x, bulge);
+            const double r = norm2(x, bulge);
             const double c = r != 0.0 ? x / r : 1.0, sn = r != 0.0 ? bulge / r : 0.0;
             if (k > lo) e[k - 1] = r;
             const double a0 = d[k], b0 = d[k + 1], o = e[k];
@@ -395,8 +440,12 @@ rt_status symeig_device(int n_, const double* A, double* w, double* V, cudaStrea
         RT_CUDA_TRY(cudaMemcpyAsync(dhi, sw.hi.data(), sizeof(int) * nsw, cudaMemcpyHostToDevice, s));
         RT_CUDA_TRY(cudaMemcpyAsync(dfirst, sw.first.data(), sizeof(int64_t) * nsw, cudaMemcpyHostToDevice, s));
         RT_CUDA_TRY(cudaMemcpyAsync(drot, sw.rot.data(), sizeof(double2) * sw.rot.size(), cudaMemcpyHostToDevice, s));
-        apply_rotations_kernel<<<(unsigned)ceil_div(n, 128), 128, 0, s>>>(Q, n, dlo, dhi, dfirst, drot, nsw);
-        RT_TRY(check_launch("apply_rotations_kernel"));
+        // Passes of 32 sweeps, one systolic launch each.
+        for (int s0 = 0; s0 < nsw; s0 += 32) {
+            rot_systolic_kernel<<<(unsigned)ceil_div(n, kSysRows), kSysRows * 32, 0, s>>>(
+                Q, n, dlo, dhi, dfirst, drot, s0, std::min(32, nsw - s0));
+            RT_TRY(check_launch("rot_systolic_kernel"));
+        }
         RT_CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors above go out of scope
     }
     std::vector<int> perm(n);

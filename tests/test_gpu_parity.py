@@ -177,9 +177,7 @@ def test_empty_and_degenerate_shapes():
 
 
 # ------------------------------------------------------------ J and E_x --
-# One-pass RI-J variants by shape: (20, 12) one CTA; (100, 400) and (40, 1100) groups of 8 slabs;
-# (600, 96) 3 double2 per thread in groups of 4; (750, 33) 4 per thread with a short last group;
-# (1200, 20) 12 per thread, one slab per group; (33, 7) odd slab length: the two-pass kernels.
+# Even and odd slab lengths (16-byte and scalar J kernels), naux above the 1024 slabs of one w stage.
 @pytest.mark.parametrize("nb,naux", [(20, 12), (33, 7), (100, 400), (40, 1100), (600, 96), (750, 33), (1200, 20)])
 def test_ri_j_matches_oracle(nb, naux):
     C, B = inputs(nb, naux, seed=1)

@@ -6,8 +6,10 @@
   level, on random, degenerate, diagonal and tridiagonal matrices; only the
   lower triangle is read; bitwise repeatable.
 * rt_lapack_power (matrix_blas_lapack.rs:1004-1064) against the oracle's
-  restatement over OpenBLAS, on the reference's own test inputs and random
-  cases: 1e-12 relative (float64 product), 1e-11 (split product).
+  restatement over OpenBLAS, on the reference's own test inputs and on
+  well-conditioned random matrices up to n = 600: 1e-12 relative (float64
+  product), 1e-11 (split product); with small eigenvalues kept under negative
+  powers (ill-conditioned by construction): 1e-10.
 * rt_dspgvx (matrix_blas_lapack.rs:1096-1147) against the oracle's dspgvx:
   eigenvalues 1e-12 relative, eigenvectors up to sign 1e-10, B-orthonormal.
 """
@@ -101,9 +103,26 @@ def test_lapack_power_on_the_reference_test_inputs(name, form, tol):
     assert np.max(np.abs(host(out, (n, n)) - ref)) / np.max(np.abs(ref)) < tol * (10 if name.endswith("3x3") else 1)
 
 
-@pytest.mark.parametrize("n,p,threshold", [(40, -0.5, 2e-4), (120, 0.5, 0.0), (300, -1.0, 1e-3), (64, 2.0, -1.0)])
+@pytest.mark.parametrize("n,p", [(64, -0.5), (600, -0.5), (600, 0.5), (300, -1.0), (300, 2.0)])
 @pytest.mark.parametrize("form,tol", [("fp64", 1e-12), ("split", 1e-11)])
-def test_lapack_power_random_matches_oracle(n, p, threshold, form, tol):
+def test_lapack_power_matches_oracle(n, p, form, tol):
+    # Eigenvalues in [0.5, 3] (a metric-like, well-conditioned matrix): two correct eigensolvers agree
+    # to a few ulps of the result.
+    ev = np.random.default_rng(n).uniform(0.5, 3.0, n)
+    S = with_spectrum(ev, n + 1)
+    ref, kept_ref = oracle.lapack_power(S, p, 1e-10)
+    out, kept = rt.lapack_power(dev(S), n, p, 1e-10, form=form)
+    rt.sync_status()
+    assert kept == kept_ref == n
+    assert np.max(np.abs(host(out, (n, n)) - ref)) / np.max(np.abs(ref)) < tol
+
+
+@pytest.mark.parametrize("n,p,threshold", [(40, -0.5, 2e-4), (120, 0.5, 0.0), (300, -1.0, 1e-3), (64, 2.0, -1.0)])
+@pytest.mark.parametrize("form", ["fp64", "split"])
+def test_lapack_power_threshold_matches_oracle(n, p, threshold, form):
+    # Four eigenvalues in 1e-6 .. 5e-4 beside [0.5, 3]: the threshold drops some of them, as the
+    # reference zeroes their columns.  A kept eigenvalue ev under a negative power amplifies any
+    # eigensolver's rounding by about ev^(p-1) / gap, so the tolerance here is 1e-10.
     rng = np.random.default_rng(n)
     ev = np.concatenate([rng.uniform(0.5, 3.0, n - 4), [1e-6, 2e-5, 1e-4, 5e-4]])
     S = with_spectrum(ev, n + 1)
@@ -111,7 +130,7 @@ def test_lapack_power_random_matches_oracle(n, p, threshold, form, tol):
     out, kept = rt.lapack_power(dev(S), n, p, threshold, form=form)
     rt.sync_status()
     assert kept == kept_ref
-    assert np.max(np.abs(host(out, (n, n)) - ref)) / np.max(np.abs(ref)) < tol * max(1.0, n / 64)
+    assert np.max(np.abs(host(out, (n, n)) - ref)) / np.max(np.abs(ref)) < 1e-10
 
 
 @pytest.mark.parametrize("n,k", [(60, 12), (200, 50), (5, 5)])
