@@ -175,6 +175,24 @@ rt_status rt_ri_ov_k(const double* C, const double* B, int nb, int naux, int noc
 rt_status rt_ri_ov_k_fp64_noalloc(const double* C, const double* B, int nb, int naux, int nocc, int nvir, double* ov,
                                   double* K, void* stream);
 
+/* ri3ao prepared for repeated split-form ov + RI-K: its BF16 digit planes and
+ * row exponents as the A operand of the half-transform X^P = B^P C_occ, made
+ * once and reused by every rt_ri_ov_k_prepared call with new orbitals.  In
+ * REST's SCF loop ri3fn is fixed while C changes, so each iteration then skips
+ * slicing the three-centre tensor (it still reads its digit planes).  No
+ * counterpart in the reference; the results are bitwise those of rt_ri_ov_k
+ * in the split form with the same nslices.  The planes take about
+ * 2 nslices nb^2 naux bytes on the device that made them
+ * (rt_ri3ao_prepared_bytes), held until rt_ri3ao_release.  rt_ri3ao_prepare
+ * synchronises `stream`, so the handle is ready on return; B is not referenced
+ * afterwards. */
+typedef struct rt_ri3ao_prepared rt_ri3ao_prepared;
+rt_status rt_ri3ao_prepare(const double* B, int nb, int naux, int nslices, rt_ri3ao_prepared** out, void* stream);
+rt_status rt_ri3ao_prepared_bytes(const rt_ri3ao_prepared* h, long long* bytes);
+rt_status rt_ri_ov_k_prepared(const rt_ri3ao_prepared* h, const double* C, int nocc, int nvir, double* ov, double* K,
+                              void* stream);
+rt_status rt_ri3ao_release(rt_ri3ao_prepared* h);
+
 /* One molecule of a batch: device pointers and sizes as for rt_ri_ov_k. */
 typedef struct {
     const double* C;

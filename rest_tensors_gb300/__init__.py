@@ -103,6 +103,14 @@ def lib() -> ctypes.CDLL:
     L.rt_ri_ov_k_host_symmetric.argtypes = [vp, vp, c_int, c_int, c_int, c_int, vp, vp, c_int, c_int, vp]
     L.rt_ri_ov_k_fp64_noalloc.restype = c_int
     L.rt_ri_ov_k_fp64_noalloc.argtypes = [vp, vp, c_int, c_int, c_int, c_int, vp, vp, vp]
+    L.rt_ri3ao_prepare.restype = c_int
+    L.rt_ri3ao_prepare.argtypes = [vp, c_int, c_int, c_int, ctypes.POINTER(vp), vp]
+    L.rt_ri3ao_prepared_bytes.restype = c_int
+    L.rt_ri3ao_prepared_bytes.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
+    L.rt_ri_ov_k_prepared.restype = c_int
+    L.rt_ri_ov_k_prepared.argtypes = [vp, vp, c_int, c_int, vp, vp, vp]
+    L.rt_ri3ao_release.restype = c_int
+    L.rt_ri3ao_release.argtypes = [vp]
     L.rt_ri_j.restype = c_int
     L.rt_ri_j.argtypes = [vp, vp, c_int, c_int, vp, vp, vp]
     L.rt_ri_exchange_energy.restype = c_int
@@ -415,6 +423,52 @@ def ri_ov_k_fp64_noalloc(C, B, nb: int, naux: int, nocc: int, nvir: int, ov=None
                                          nocc, nvir, _dptr(ov, nocc * nvir * naux, "ov"), _dptr(K, nb * nb, "K"),
                                          _stream(stream)))
     return ov, K
+
+
+class Ri3aoPrepared:
+    """ri3ao sliced once into split-form digit planes (rt_ri3ao_prepare) for repeated ov + RI-K with new
+    orbitals, as in an SCF loop where ri3fn is fixed while C changes.  Holds about 2 nslices nb^2 naux bytes of
+    device memory until release() (or garbage collection)."""
+
+    def __init__(self, B, nb: int, naux: int, nslices: int = DEFAULT_NSLICES, stream=None):
+        self.h = None
+        h = ctypes.c_void_p()
+        _check(lib().rt_ri3ao_prepare(_dptr(B, nb * nb * naux, "B"), nb, naux, nslices, ctypes.byref(h),
+                                      _stream(stream)))
+        self.h, self.nb, self.naux, self.nslices = h, nb, naux, nslices
+
+    def nbytes(self) -> int:
+        b = ctypes.c_longlong()
+        _check(lib().rt_ri3ao_prepared_bytes(self.h, ctypes.byref(b)))
+        return b.value
+
+    def ri_ov_k(self, C, nocc: int, nvir: int, ov=None, K=None, stream=None, want_ov: bool = True,
+                want_k: bool = True):
+        """ov (i,a,P) and K [nb, nb] for orbitals C, from the prepared digit planes."""
+        import torch
+
+        if self.h is None:
+            raise ValueError("Ri3aoPrepared: already released")
+        nb, naux = self.nb, self.naux
+        if want_ov and ov is None:
+            ov = torch.empty(max(nocc * nvir * naux, 1), dtype=torch.float64, device=C.device)
+        if want_k and K is None:
+            K = torch.empty(nb * nb, dtype=torch.float64, device=C.device)
+        _check(lib().rt_ri_ov_k_prepared(self.h, _dptr(C, nb * (nocc + nvir), "C"), nocc, nvir,
+                                         _dptr(ov, nocc * nvir * naux, "ov") if want_ov else None,
+                                         _dptr(K, nb * nb, "K") if want_k else None, _stream(stream)))
+        return ov, K
+
+    def release(self) -> None:
+        if getattr(self, "h", None) is not None:
+            lib().rt_ri3ao_release(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
 
 
 def ri_ov_k_batched(problems, form: str = "split", nslices: int = DEFAULT_NSLICES, tuning=None, stream=None):

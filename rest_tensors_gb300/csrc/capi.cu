@@ -515,6 +515,103 @@ rt_status rt_ri_ov_k_batched(const rt_ri_problem* probs, int nprob, int form, in
     return RT_OK;
 }
 
+}  // extern "C"
+
+// ------------------------------------------------ prepared ri3ao (SCF reuse) --
+
+// Digit planes and row exponents of ri3ao as the A operand of the half-transform
+// X^P = B^P C_occ, kept on the device that made them.
+struct rt_ri3ao_prepared {
+    int nb = 0, naux = 0, nslices = 0, device = -1;
+    uint16_t* planes = nullptr;
+    int* emax = nullptr;
+    size_t plane_bytes = 0;
+};
+
+extern "C" {
+
+rt_status rt_ri3ao_prepare(const double* B, int nb, int naux, int nslices, rt_ri3ao_prepared** out, void* stream) {
+    NvtxRange nvtx_range("rt_ri3ao_prepare");
+    RT_REQUIRE(out, "rt_ri3ao_prepare: null handle pointer");
+    *out = nullptr;
+    RT_REQUIRE(nb > 0 && naux > 0, "rt_ri3ao_prepare: nb and naux must be positive");
+    RT_REQUIRE(nslices >= 3 && nslices <= 8, "rt_ri3ao_prepare: nslices must be in 3..8");
+    RT_REQUIRE(B, "rt_ri3ao_prepare: null ri3ao");
+    cudaStream_t s = (cudaStream_t)stream;
+    const int64_t rows = (int64_t)nb * naux;
+    auto* h = new rt_ri3ao_prepared;
+    h->nb = nb; h->naux = naux; h->nslices = nslices;
+    h->plane_bytes = oz_plane_bytes(rows, nb, nslices);
+    auto fail = [&](rt_status st) {
+        if (h->planes) cudaFree(h->planes);
+        if (h->emax) cudaFree(h->emax);
+        delete h;
+        return st;
+    };
+    cudaError_t e = cudaGetDevice(&h->device);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&h->planes, h->plane_bytes);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&h->emax, sizeof(int) * (size_t)rows);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        const rt_status st = e == cudaErrorMemoryAllocation ? RT_ERR_NO_MEMORY : RT_ERR_CUDA;
+        set_error(st, "rt_ri3ao_prepare: %zu bytes of digit planes: %s", h->plane_bytes, cudaGetErrorString(e));
+        return fail(st);
+    }
+    rt_status st = error_word_reset(s);
+    if (st != RT_OK) return fail(st);
+    OzOperand A;  // rows (mu, P), k = nu: B[mu + nb nu + nb^2 P], as in x_product
+    A.p = B; A.rows = rows; A.div = nb; A.s0 = 1; A.s1 = (int64_t)nb * nb; A.sk = nb;
+    st = oz_slice_into(A, nb, nslices, h->planes, h->emax, s);
+    if (st == RT_OK) st = error_word_check(s, "rt_ri3ao_prepare");  // synchronises: the handle is ready
+    if (st != RT_OK) return fail(st);
+    *out = h;
+    return RT_OK;
+}
+
+rt_status rt_ri3ao_prepared_bytes(const rt_ri3ao_prepared* h, long long* bytes) {
+    RT_REQUIRE(h && bytes, "rt_ri3ao_prepared_bytes: null argument");
+    *bytes = (long long)(h->plane_bytes + sizeof(int) * (size_t)h->nb * h->naux);
+    return RT_OK;
+}
+
+rt_status rt_ri_ov_k_prepared(const rt_ri3ao_prepared* h, const double* C, int nocc, int nvir, double* ov, double* K,
+                              void* stream) {
+    NvtxRange nvtx_range("rt_ri_ov_k_prepared");
+    RT_REQUIRE(h, "rt_ri_ov_k_prepared: null handle");
+    RT_REQUIRE(nocc >= 0 && nvir >= 0, "rt_ri_ov_k_prepared: negative dimension");
+    int dev = -1;
+    RT_CUDA_TRY(cudaGetDevice(&dev));
+    RT_REQUIRE(dev == h->device, "rt_ri_ov_k_prepared: handle made on device %d, current device %d", h->device, dev);
+    cudaStream_t s = (cudaStream_t)stream;
+    const int nb = h->nb, naux = h->naux, S = h->nslices;
+    if (K && nocc == 0) RT_CUDA_TRY(cudaMemsetAsync(K, 0, sizeof(double) * nb * (size_t)nb, s));
+    if (nocc == 0) return RT_OK;
+    RT_REQUIRE(C, "rt_ri_ov_k_prepared: null C");
+    const int64_t per = (int64_t)nb * nocc;
+    ScratchBuf xb;
+    RT_TRY(scratch_alloc(xb, sizeof(double) * (size_t)(per * naux), s));
+    double* X = xb.as<double>();
+    OzGemm g = x_product(C, nullptr, nb, naux, nocc, X, S);
+    g.a_planes = h->planes;
+    g.a_emax = h->emax;
+    RT_TRY(oz_gemm(g, s));
+    if (ov && nvir > 0) RT_TRY(oz_gemm(ov_product(C, nb, naux, nocc, nvir, X, ov, S), s));
+    if (K) RT_TRY(ri_k_from_x(X, nb, nocc, naux, K, RT_FORM_SPLIT, S, s));
+    return RT_OK;
+}
+
+rt_status rt_ri3ao_release(rt_ri3ao_prepared* h) {
+    if (!h) return RT_OK;
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (cur != h->device) cudaSetDevice(h->device);
+    cudaFree(h->planes);
+    cudaFree(h->emax);
+    if (cur != h->device && cur >= 0) cudaSetDevice(cur);
+    delete h;
+    return RT_OK;
+}
+
 rt_status rt_ri_j(const double* B, const double* D, int nb, int naux, double* w, double* J, void* stream) {
     NvtxRange nvtx_range("rt_ri_j");
     RT_REQUIRE(nb >= 0 && naux >= 0, "rt_ri_j: negative dimension");

@@ -900,7 +900,9 @@ bool can_fuse_a(const OzOperand& A, bool reuse) {
 }
 
 struct Sliced {
-    ScratchBuf planes, emax;
+    ScratchBuf planes, emax;  // owned scratch (unused when the planes come from a prepared operand)
+    uint16_t* pl = nullptr;   // the digit planes [tiles][Kb][S][T*16]
+    int* em = nullptr;        // row exponents
     int64_t tiles = 0, Kb = 0;
     int T = 0;
 };
@@ -984,38 +986,51 @@ rt_status flush_slices(SliceQueue& q, cudaStream_t stream) {
 
 // Digit planes of one operand.  With a queue, the one-pass cases are recorded
 // there (their planes allocated now) and launched later by flush_slices.
+// Digit-plane bytes of an operand of `rows` rows sliced in tiles of T rows.
+inline size_t plane_bytes(int64_t rows, int64_t K, int T, int S) {
+    return (size_t)ceil_div(rows, T) * T * (size_t)ceil_div(K, KB) * KB * 2 * S;
+}
+
+// With ext_planes / ext_emax the digits go to caller-owned memory of
+// plane_bytes(...) and op.rows ints (a prepared operand), else to scratch.
 template <int S>
 rt_status slice_operand(const Operand& op, int64_t K, int T, Sliced& out, cudaStream_t stream,
-                        SliceQueue* queue = nullptr) {
+                        SliceQueue* queue = nullptr, uint16_t* ext_planes = nullptr, int* ext_emax = nullptr) {
     out.T = T;
     out.tiles = ceil_div(op.rows, T);
     out.Kb = ceil_div(K, KB);
-    const size_t plane_bytes = (size_t)out.tiles * T * (size_t)out.Kb * KB * 2 * S;
-    RT_TRY(scratch_alloc(out.planes, plane_bytes, stream));
-    RT_TRY(scratch_alloc(out.emax, sizeof(int) * (size_t)std::max<int64_t>(op.rows, 1), stream));
+    if (ext_planes) {
+        out.pl = ext_planes;
+        out.em = ext_emax;
+    } else {
+        RT_TRY(scratch_alloc(out.planes, plane_bytes(op.rows, K, T, S), stream));
+        RT_TRY(scratch_alloc(out.emax, sizeof(int) * (size_t)std::max<int64_t>(op.rows, 1), stream));
+        out.pl = out.planes.as<uint16_t>();
+        out.em = out.emax.as<int>();
+    }
     unsigned int* err = error_word_device();
     RT_REQUIRE(err != nullptr, "oz: device error word unavailable");
     SliceArgs sa{};
     sa.src = op; sa.K = K; sa.T = T; sa.tiles = out.tiles; sa.Kb = out.Kb;
-    sa.out = out.planes.as<uint16_t>(); sa.emax = out.emax.as<int>(); sa.err = err;
+    sa.out = out.pl; sa.emax = out.em; sa.err = err;
     if (op.sk == 1 && out.Kb * KB <= 128 * 5) {
         const unsigned grid = (unsigned)(out.tiles * T / kFusedRows);
         if (queue) {
-            queue->jobs.push_back(SliceJob{0, (int)std::min<int64_t>(ceil_div(out.Kb, 8), 5), sa, out.emax.as<int>(),
+            queue->jobs.push_back(SliceJob{0, (int)std::min<int64_t>(ceil_div(out.Kb, 8), 5), sa, out.em,
                                            (int64_t)grid});
             return RT_OK;
         }
         switch ((int)ceil_div(out.Kb, 8)) {
-            case 1: slice_contig_rowmax_kernel<S, 1><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
-            case 2: slice_contig_rowmax_kernel<S, 2><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
-            case 3: slice_contig_rowmax_kernel<S, 3><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
-            case 4: slice_contig_rowmax_kernel<S, 4><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
-            default: slice_contig_rowmax_kernel<S, 5><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
+            case 1: slice_contig_rowmax_kernel<S, 1><<<grid, 256, 0, stream>>>(sa, out.em); break;
+            case 2: slice_contig_rowmax_kernel<S, 2><<<grid, 256, 0, stream>>>(sa, out.em); break;
+            case 3: slice_contig_rowmax_kernel<S, 3><<<grid, 256, 0, stream>>>(sa, out.em); break;
+            case 4: slice_contig_rowmax_kernel<S, 4><<<grid, 256, 0, stream>>>(sa, out.em); break;
+            default: slice_contig_rowmax_kernel<S, 5><<<grid, 256, 0, stream>>>(sa, out.em); break;
         }
         RT_TRY(check_launch("slice_contig_rowmax_kernel"));
     } else if (op.sk == 1) {
         const int64_t warps = std::min<int64_t>(op.rows, 64ll * sm_count());
-        emax_contig_kernel<<<(unsigned)ceil_div(warps * 32, 256), 256, 0, stream>>>(op, K, out.emax.as<int>(), err);
+        emax_contig_kernel<<<(unsigned)ceil_div(warps * 32, 256), 256, 0, stream>>>(op, K, out.em, err);
         RT_TRY(check_launch("emax_contig_kernel"));
         dim3 grid((unsigned)out.tiles, (unsigned)ceil_div(K, SK));
         slice_contig_kernel<S><<<grid, 256, 0, stream>>>(sa);
@@ -1025,16 +1040,16 @@ rt_status slice_operand(const Operand& op, int64_t K, int T, Sliced& out, cudaSt
         const unsigned grid = (unsigned)(out.tiles * T / RR);
         if (queue) {
             const int nb = (int)ceil_div(out.Kb * KB, 8 * KQN);
-            queue->jobs.push_back(SliceJob{1, nb <= 4 ? nb : 5, sa, out.emax.as<int>(), (int64_t)grid});
+            queue->jobs.push_back(SliceJob{1, nb <= 4 ? nb : 5, sa, out.em, (int64_t)grid});
             return RT_OK;
         }
         switch ((int)ceil_div(out.Kb * KB, 8 * KQN)) {
-            case 1: slice_strided_rowmax_kernel<S, 1, RR><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
-            case 2: slice_strided_rowmax_kernel<S, 2, RR><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
-            case 3: slice_strided_rowmax_kernel<S, 3, RR><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
-            case 4: slice_strided_rowmax_kernel<S, 4, RR><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
+            case 1: slice_strided_rowmax_kernel<S, 1, RR><<<grid, 256, 0, stream>>>(sa, out.em); break;
+            case 2: slice_strided_rowmax_kernel<S, 2, RR><<<grid, 256, 0, stream>>>(sa, out.em); break;
+            case 3: slice_strided_rowmax_kernel<S, 3, RR><<<grid, 256, 0, stream>>>(sa, out.em); break;
+            case 4: slice_strided_rowmax_kernel<S, 4, RR><<<grid, 256, 0, stream>>>(sa, out.em); break;
             default: slice_strided_rowmax_kernel<S, (640 + 8 * KQN - 1) / (8 * KQN), RR>
-                         <<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
+                         <<<grid, 256, 0, stream>>>(sa, out.em); break;
         }
         RT_TRY(check_launch("slice_strided_rowmax_kernel"));
     } else if (op.s0 == 1 && out.Kb * KB <= 1280) {
@@ -1043,16 +1058,16 @@ rt_status slice_operand(const Operand& op, int64_t K, int T, Sliced& out, cudaSt
         constexpr int RR = kStridedRowsWide, KQN = 256 / RR;
         const unsigned grid = (unsigned)(out.tiles * T / RR);
         switch ((int)ceil_div(out.Kb * KB, 8 * KQN)) {
-            case 3: slice_strided_rowmax_kernel<S, 3, RR><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
-            case 4: slice_strided_rowmax_kernel<S, 4, RR><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
-            default: slice_strided_rowmax_kernel<S, 5, RR><<<grid, 256, 0, stream>>>(sa, out.emax.as<int>()); break;
+            case 3: slice_strided_rowmax_kernel<S, 3, RR><<<grid, 256, 0, stream>>>(sa, out.em); break;
+            case 4: slice_strided_rowmax_kernel<S, 4, RR><<<grid, 256, 0, stream>>>(sa, out.em); break;
+            default: slice_strided_rowmax_kernel<S, 5, RR><<<grid, 256, 0, stream>>>(sa, out.em); break;
         }
         RT_TRY(check_launch("slice_strided_rowmax_kernel"));
     } else if (op.s0 == 1) {
-        RT_CUDA_TRY(cudaMemsetAsync(out.emax.p, 0, sizeof(int) * (size_t)op.rows, stream));
+        RT_CUDA_TRY(cudaMemsetAsync(out.em, 0, sizeof(int) * (size_t)op.rows, stream));
         const int64_t kspan = 512;
         dim3 g1((unsigned)ceil_div(op.rows, 256), (unsigned)ceil_div(K, kspan));
-        emax_strided_kernel<<<g1, 256, 0, stream>>>(op, K, kspan, out.emax.as<int>(), err);
+        emax_strided_kernel<<<g1, 256, 0, stream>>>(op, K, kspan, out.em, err);
         RT_TRY(check_launch("emax_strided_kernel"));
         dim3 grid((unsigned)out.tiles, (unsigned)ceil_div(K, SK));
         slice_strided_kernel<S><<<grid, 256, 0, stream>>>(sa);
@@ -1097,20 +1112,28 @@ rt_status prepare(const OzGemm& g, Prepared& P, cudaStream_t stream, SliceQueue*
     Sliced& sa = P.sa;
     Sliced& sb = P.sb;
     const bool reuse = g.b_is_a;
-    const bool fused = g.allow_fuse && can_fuse_a(g.A, reuse);
+    const bool fused = !g.a_planes && g.allow_fuse && can_fuse_a(g.A, reuse);
     P.fused = fused;
     // Slicing is HBM-bound: count bytes (8 read + 2*S written per element; the
     // fused path only reads A's float64 once for its row exponents).
-    const double slice_bytes = fused ? (double)A.rows * g.K * 8.0 + (double)B.rows * g.K * (8.0 + 2.0 * S)
-                                     : (double)(A.rows + (reuse ? 0 : B.rows)) * (double)g.K * (8.0 + 2.0 * S);
+    const double slice_bytes = g.a_planes ? (reuse ? 0.0 : (double)B.rows * g.K * (8.0 + 2.0 * S))
+                               : fused ? (double)A.rows * g.K * 8.0 + (double)B.rows * g.K * (8.0 + 2.0 * S)
+                                       : (double)(A.rows + (reuse ? 0 : B.rows)) * (double)g.K * (8.0 + 2.0 * S);
     // With a queue, the caller times the grouped slicing itself.
     if (!queue) prof_begin(PROF_OZ_SLICE, stream);
-    if (fused) {
+    if (g.a_planes) {  // A sliced once beforehand (a prepared operand)
+        sa.T = TM;
+        sa.tiles = ceil_div(A.rows, TM);
+        sa.Kb = ceil_div(g.K, KB);
+        sa.pl = const_cast<uint16_t*>(g.a_planes);
+        sa.em = const_cast<int*>(g.a_emax);
+    } else if (fused) {
         sa.T = TM;
         sa.tiles = ceil_div(A.rows, TM);
         sa.Kb = ceil_div(g.K, KB);
         RT_TRY(scratch_alloc(sa.emax, sizeof(int) * (size_t)A.rows, stream));
-        RT_TRY(row_exponents<S>(A, g.K, sa.emax.as<int>(), stream));
+        sa.em = sa.emax.as<int>();
+        RT_TRY(row_exponents<S>(A, g.K, sa.em, stream));
     } else {
         RT_TRY(slice_operand<S>(A, g.K, TM, sa, stream, queue));
     }
@@ -1126,26 +1149,26 @@ rt_status prepare(const OzGemm& g, Prepared& P, cudaStream_t stream, SliceQueue*
         a.a_sk = A.sk;
     }
     a.K = g.K;
-    a.a_slices = sa.planes.as<uint8_t>();
+    a.a_slices = reinterpret_cast<const uint8_t*>(sa.pl);
     a.a_s_stride = TM * KB * 2;
     a.a_kb_stride = (int64_t)S * TM * KB * 2;
     a.a_tile_stride = sa.Kb * a.a_kb_stride;
     if (reuse) {
-        a.b_slices = sa.planes.as<uint8_t>();
+        a.b_slices = reinterpret_cast<const uint8_t*>(sa.pl);
         a.b_tile2_stride = a.a_tile_stride;
         a.b_half_stride = TN * KB * 2;
         a.b_kb_stride = a.a_kb_stride;
         a.b_s_stride = a.a_s_stride;
-        a.eb = sa.emax.as<int>();
+        a.eb = sa.em;
     } else {
-        a.b_slices = sb.planes.as<uint8_t>();
+        a.b_slices = reinterpret_cast<const uint8_t*>(sb.pl);
         a.b_s_stride = TN * KB * 2;
         a.b_kb_stride = (int64_t)S * TN * KB * 2;
         a.b_half_stride = sb.Kb * a.b_kb_stride;
         a.b_tile2_stride = 2 * a.b_half_stride;
-        a.eb = sb.emax.as<int>();
+        a.eb = sb.em;
     }
-    a.ea = sa.emax.as<int>();
+    a.ea = sa.em;
     a.M = A.rows;
     a.N = B.rows;
     a.Kb = sa.Kb;
@@ -1309,6 +1332,28 @@ rt_status oz_gemm_many(const OzGemm* gs, int n, cudaStream_t stream) {
         case 8: return oz::run_many<8>(gs, n, stream);
         default:
             set_error(RT_ERR_INVALID_ARG, "nslices must be in 3..8 (got %d)", S);
+            return RT_ERR_INVALID_ARG;
+    }
+}
+
+size_t oz_plane_bytes(int64_t rows, int64_t K, int nslices) { return oz::plane_bytes(rows, K, oz::TM, nslices); }
+
+// Digit planes and row exponents of A as the A operand of later products
+// (OzGemm::a_planes / a_emax), into caller-owned memory.
+rt_status oz_slice_into(const OzOperand& A, int64_t K, int nslices, uint16_t* planes, int* emax,
+                        cudaStream_t stream) {
+    RT_REQUIRE(A.rows > 0 && K > 0 && planes && emax, "oz_slice_into: bad arguments");
+    oz::Operand op{A.p, A.rows, A.div, A.s0, A.s1, A.sk};
+    oz::Sliced sl;
+    switch (nslices) {
+        case 3: return oz::slice_operand<3>(op, K, oz::TM, sl, stream, nullptr, planes, emax);
+        case 4: return oz::slice_operand<4>(op, K, oz::TM, sl, stream, nullptr, planes, emax);
+        case 5: return oz::slice_operand<5>(op, K, oz::TM, sl, stream, nullptr, planes, emax);
+        case 6: return oz::slice_operand<6>(op, K, oz::TM, sl, stream, nullptr, planes, emax);
+        case 7: return oz::slice_operand<7>(op, K, oz::TM, sl, stream, nullptr, planes, emax);
+        case 8: return oz::slice_operand<8>(op, K, oz::TM, sl, stream, nullptr, planes, emax);
+        default:
+            set_error(RT_ERR_INVALID_ARG, "nslices must be in 3..8 (got %d)", nslices);
             return RT_ERR_INVALID_ARG;
     }
 }

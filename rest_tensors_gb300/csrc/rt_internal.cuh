@@ -160,8 +160,14 @@ struct OzGemm {
     // the fused form trades speed for memory.
     bool allow_fuse = false;
     int chunks_per_item = 0;  // >0: exact chunks per work item (split-K granularity); 0: fill whole waves
+    // A already sliced by oz_slice_into with the same nslices (A's layout then only sets rows and K).
+    const uint16_t* a_planes = nullptr;
+    const int* a_emax = nullptr;
 };
 rt_status oz_gemm(const OzGemm& g, cudaStream_t stream);
+// Bytes of the digit planes of an A operand (rows x K, nslices digits), and the slicing into caller memory.
+size_t oz_plane_bytes(int64_t rows, int64_t K, int nslices);
+rt_status oz_slice_into(const OzOperand& A, int64_t K, int nslices, uint16_t* planes, int* emax, cudaStream_t stream);
 // Several independent products with the same slice count: one slicing pass
 // each, then as few grouped persistent GEMM launches as possible.
 rt_status oz_gemm_many(const OzGemm* gs, int n, cudaStream_t stream);
