@@ -743,18 +743,34 @@ __global__ void __launch_bounds__(256) host_read_kernel(const double2* __restric
     for (; i < n2; i += stride) dst[i] = src[i];
 }
 
+// Device view of the page-locked host range h[0, n), or nullptr when the range
+// is not page-locked as a whole: its first and its last element must both be
+// pinned, with device addresses n - 1 elements apart (one registration, or
+// registrations mapped contiguously).  Anything else (pageable memory, a range
+// only partly registered) goes through the copy engine.
+const double* pinned_view(const double* h, int64_t n) {
+    if (n <= 0) return nullptr;
+    cudaPointerAttributes a{}, b{};
+    if (cudaPointerGetAttributes(&a, h) != cudaSuccess || a.type != cudaMemoryTypeHost || !a.devicePointer ||
+        cudaPointerGetAttributes(&b, h + (n - 1)) != cudaSuccess || b.type != cudaMemoryTypeHost ||
+        !b.devicePointer ||
+        (const double*)b.devicePointer != (const double*)a.devicePointer + (n - 1)) {
+        cudaGetLastError();  // pageable memory has no device view
+        return nullptr;
+    }
+    return static_cast<const double*>(a.devicePointer);
+}
+
 // Host-to-device copy of n doubles: the kernel above for 16-byte-aligned
 // pinned memory, the copy engine otherwise.
 rt_status copy_slabs_h2d(const double* hB, double* dB, int64_t n, cudaStream_t s) {
-    cudaPointerAttributes pa{};
-    if ((n & 1) == 0 && ((uintptr_t)hB & 15) == 0 && ((uintptr_t)dB & 15) == 0 &&
-        cudaPointerGetAttributes(&pa, hB) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer &&
-        ((uintptr_t)pa.devicePointer & 15) == 0) {
-        host_read_kernel<<<2 * sm_count(), 256, 0, s>>>(static_cast<const double2*>(pa.devicePointer),
+    const double* view = ((n & 1) == 0 && ((uintptr_t)hB & 15) == 0 && ((uintptr_t)dB & 15) == 0)
+                             ? pinned_view(hB, n) : nullptr;
+    if (view && ((uintptr_t)view & 15) == 0) {
+        host_read_kernel<<<2 * sm_count(), 256, 0, s>>>(reinterpret_cast<const double2*>(view),
                                                          reinterpret_cast<double2*>(dB), n / 2);
         return check_launch("host_read_kernel");
     }
-    cudaGetLastError();  // pageable memory has no device view
     RT_CUDA_TRY(cudaMemcpyAsync(dB, hB, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, s));
     return RT_OK;
 }
@@ -765,15 +781,12 @@ rt_status copy_slabs_h2d(const double* hB, double* dB, int64_t n, cudaStream_t s
 // Everything below the diagonal is then mirrored on the device.
 rt_status copy_symmetric_slabs(const double* hB, double* dB, int nb, int64_t np, cudaStream_t s) {
     const int nbt = (nb + 31) / 32;
-    cudaPointerAttributes pa{};
-    if (cudaPointerGetAttributes(&pa, hB) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer) {
-        const double* dev_view = static_cast<const double*>(pa.devicePointer);
+    if (const double* dev_view = pinned_view(hB, (int64_t)nb * nb * np)) {
         // Two CTAs per SM keep enough host reads in flight to fill the link (1, 0.5 and
         // 0.1 per SM left it idle; 4 and 8 per SM took SMs from the transform).
         sym_gather_kernel<<<2 * sm_count(), dim3(32, 8), 0, s>>>(dev_view, dB, nb, nbt, np);
         return check_launch("sym_gather_kernel");
     }
-    cudaGetLastError();  // pageable memory: no device view, take the copy path
     for (int J = 0; J < nbt; ++J) {
         const int c0 = 32 * J, c1 = std::min(nb, c0 + 32);
         const int rows = std::min(nb, c0 + 32);
