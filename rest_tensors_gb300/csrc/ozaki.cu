@@ -479,6 +479,86 @@ __device__ __forceinline__ double scale_pow2(int64_t v, int ex) {
     return ldexp(r, ex);
 }
 
+// ------------------------------------------------- accumulator drain --
+// Group g of a chunk holds, per column, the exact integer sum v_g (in FP32) of
+// its digit-pair products; it enters the int64 result as v_g * 2^sh_g with
+// sh_g = 7 (S-1-g) - R.  Negative shifts (the overflow guard R) round to
+// nearest, ties to even.
+
+// d = a * b + c with a 32 x 32 -> 64-bit signed product.
+__device__ __forceinline__ int64_t mad_wide(int32_t a, int32_t b, int64_t c) {
+    int64_t d;
+    asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(d) : "r"(a), "r"(b), "l"(c));
+    return d;
+}
+
+// acc[j] += p(j) * 2^sh for 32-bit integers p(j) and a shift 0 <= sh <= 62 that
+// is the same for every j: one multiply-add below 2^31, the high word alone
+// from 2^32 up (the low word of p * 2^sh is zero there).
+template <int HC, class P>
+__device__ __forceinline__ void add_shifted(int64_t (&acc)[HC], int sh, P p) {
+    if (sh <= 30) {
+        const int32_t mul = 1 << sh;
+#pragma unroll
+        for (int j = 0; j < HC; ++j) acc[j] = mad_wide(p(j), mul, acc[j]);
+    } else if (sh >= 32) {
+#pragma unroll
+        for (int j = 0; j < HC; ++j) acc[j] += (int64_t)((uint64_t)((uint32_t)p(j) << (sh - 32)) << 32);
+    } else {
+#pragma unroll
+        for (int j = 0; j < HC; ++j) acc[j] += (int64_t)p(j) << sh;
+    }
+}
+
+template <int HC>
+__device__ __forceinline__ void add_group(int64_t (&acc)[HC], const uint32_t (&r)[HC], int sh) {
+    if (sh >= 0) {
+        add_shifted<HC>(acc, sh, [&](int j) { return __float2int_rn(__uint_as_float(r[j])); });
+    } else {
+        const int s = -sh;
+        const int64_t half = (1ll << (s - 1)) - 1;
+#pragma unroll
+        for (int j = 0; j < HC; ++j) {
+            const int64_t v = (int64_t)__float2int_rn(__uint_as_float(r[j]));
+            acc[j] += (v + half + ((v >> s) & 1)) >> s;
+        }
+    }
+}
+
+// Groups g and g+1 (g+1 < S), or g alone when it is the last.  Where group
+// g+1's shift sh is not negative, (v_g << (sh+7)) + (v_{g+1} << sh) is formed
+// as (128 v_g + v_{g+1}) << sh with the bracket in 32 bits, which is exact: an
+// exact chunk has n <= (2^24 - 1) / (S 65^2) terms, so |v_g| <= (g+1) 65^2 n
+// < (g+1) 2^24 / S and |128 v_g + v_{g+1}| < 2^24 (128 - 127/S) < 2^31.
+template <int S, int HC>
+__device__ __forceinline__ void add_group_pair(int64_t (&acc)[HC], const uint32_t (&x)[HC], const uint32_t (&y)[HC],
+                                               int g, int R) {
+    if (g + 1 >= S) {
+        add_group<HC>(acc, x, 7 * (S - 1 - g) - R);
+        return;
+    }
+    const int sh = 7 * (S - 2 - g) - R;
+    if (sh >= 0) {
+        add_shifted<HC>(acc, sh, [&](int j) {
+            return __float2int_rn(__uint_as_float(x[j])) * 128 + __float2int_rn(__uint_as_float(y[j]));
+        });
+    } else {
+        add_group<HC>(acc, x, sh + 7);
+        add_group<HC>(acc, y, sh);
+    }
+}
+
+// Issue the tensor-memory loads of groups g and g+1 (g alone when g+1 == S)
+// for this thread's lane and HC columns starting at col.
+__device__ __forceinline__ void tmem_ld_cols(uint32_t taddr, uint32_t (&r)[16]) { ptx::tmem_ld16(taddr, r); }
+__device__ __forceinline__ void tmem_ld_cols(uint32_t taddr, uint32_t (&r)[32]) { ptx::tmem_ld32(taddr, r); }
+
+template <int S, int HC>
+__device__ __forceinline__ void load_group_pair(uint32_t col, int g, uint32_t (&x)[HC], uint32_t (&y)[HC]) {
+    tmem_ld_cols(col + (uint32_t)(g * TN), x);
+    if (g + 1 < S) tmem_ld_cols(col + (uint32_t)((g + 1) * TN), y);
+}
+
 __device__ __forceinline__ int64_t out_addr(const OutMap& o, int64_t m, int64_t n) {
     return (m % o.md) * o.ms0 + (m / o.md) * o.ms1 + (n % o.nd) * o.ns0 + (n / o.nd) * o.ns1;
 }
@@ -785,31 +865,40 @@ __global__ void __launch_bounds__(FUSED ? NTHREADS_FUSED : NTHREADS, 1)
             for (int64_t c = c0; c < c1; ++c, ++cc) {
                 if (!ptx::mbar_wait(acc_full, (uint32_t)(cc & 1), a.err)) { ok = false; break; }
                 ptx::tc_fence_after();
+                // Groups are read in pairs (one per load round with 16 columns per
+                // thread; single groups with 32, for registers).  The tensor memory is
+                // handed back to the MMA warp as soon as the last load has landed, before
+                // the last conversion.
+                const uint32_t col = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(h * HC);
+                uint32_t x[HC];
+                if constexpr (HC <= 16) {
+                    uint32_t y[HC];
 #pragma unroll 1
-                for (int g = 0; g < S; ++g) {
-                    const int sh = 7 * (S - 1 - g) - a.R;
-                    uint32_t r0[16], r1[16];
-                    const uint32_t col = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(g * TN + h * HC);
-                    ptx::tmem_ld16(col, r0);
-                    if constexpr (HC > 16) ptx::tmem_ld16(col + 16, r1);
-                    ptx::tmem_wait_ld();
-                    if (sh >= 0) {
-#pragma unroll
-                        for (int j = 0; j < HC; ++j)
-                            acc[j] += (int64_t)__float2int_rn(__uint_as_float(j < 16 ? r0[j] : r1[j - 16])) << sh;
-                    } else {
-                        // Right shifts round to nearest, ties to even.
-                        const int r = -sh;
-                        const int64_t half = (1ll << (r - 1)) - 1;
-#pragma unroll
-                        for (int j = 0; j < HC; ++j) {
-                            const int64_t v = (int64_t)__float2int_rn(__uint_as_float(j < 16 ? r0[j] : r1[j - 16]));
-                            acc[j] += (v + half + ((v >> r) & 1)) >> r;
+                    for (int g = 0;; g += 2) {
+                        load_group_pair<S, HC>(col, g, x, y);
+                        ptx::tmem_wait_ld();
+                        const bool last = g + 2 >= S;
+                        if (last) {
+                            ptx::tc_fence_before();
+                            ptx::mbar_arrive(acc_empty);
                         }
+                        add_group_pair<S, HC>(acc, x, y, g, a.R);
+                        if (last) break;
+                    }
+                } else {
+#pragma unroll 1
+                    for (int g = 0;; ++g) {
+                        tmem_ld_cols(col + (uint32_t)(g * TN), x);
+                        ptx::tmem_wait_ld();
+                        const bool last = g + 1 >= S;
+                        if (last) {
+                            ptx::tc_fence_before();
+                            ptx::mbar_arrive(acc_empty);
+                        }
+                        add_group<HC>(acc, x, 7 * (S - 1 - g) - a.R);
+                        if (last) break;
                     }
                 }
-                ptx::tc_fence_before();
-                ptx::mbar_arrive(acc_empty);
             }
             if (!ok || m >= a.M) continue;
             const int64_t n0 = tn * TN + h * HC;
