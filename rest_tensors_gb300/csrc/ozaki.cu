@@ -64,15 +64,60 @@ __host__ __device__ constexpr int stage_bytes(int S, bool fused = false) {
 __host__ __device__ constexpr int num_stages(int S, bool fused = false) {
     return kSmemBudget / stage_bytes(S, fused) > 6 ? 6 : kSmemBudget / stage_bytes(S, fused);
 }
-// Longest contraction chunk whose group sums stay exact in FP32, in k-blocks.
-__host__ __device__ constexpr int chunk_kblocks(int S) { return (int)(((1 << 24) - 1) / (S * 65 * 65) / KB); }
+__host__ __device__ constexpr int tmem_cols(int S) { return S * TN <= 256 ? 256 : 512; }
+
+// Accumulator groups.  The product of A digit s and B digit t (s + t <= S-1)
+// carries weight 2^(-7(s+t)) and accumulates in group g = s + t, TMEM columns
+// [g TN, (g+1) TN).  The MMAs for A digit s stack B digits t0 .. t0+nt-1 (nt <= 4)
+// along N; when (S - s) % 4 == 1 the last of them holds B digit S-1-s alone, a
+// product of the last group.  Where the allocation has a column block to spare
+// (S = 3, 5, 6, 7), those lone products with s >= 1 accumulate there instead,
+// in an extra group of the same weight as group S-1 (s = 0's MMAs must cover
+// every regular group: they start each chunk by overwriting them).  The widest
+// group then has fewer pairs, so an exact chunk is longer.
+__host__ __device__ constexpr bool extra_group(int S) { return (S + 1) * TN <= tmem_cols(S); }
+__host__ __device__ constexpr bool extra_pair(int S, int s) { return extra_group(S) && s >= 1 && (S - s) % 4 == 1; }
+// The first A digit whose lone product goes to the extra group (it starts it).
+__host__ __device__ constexpr int first_extra_pair(int S) {
+    int f = -1;
+    for (int s = S - 1; s >= 1; --s) f = extra_pair(S, s) ? s : f;
+    return f;
+}
+// Largest |product| of digits s and t: |d_0| <= 65, |d_s| <= 64 for s >= 1.
+__host__ __device__ constexpr int pair_bound(int s, int t) { return (s == 0 ? 65 : 64) * (t == 0 ? 65 : 64); }
+// Largest |sum over one k| of group g's products (g == S: the extra group).
+__host__ __device__ constexpr int group_bound(int S, int g) {
+    int b = 0;
+    for (int s = 0; s < S; ++s) {
+        const bool moved = extra_pair(S, s);
+        if (g == S ? moved : (g - s >= 0 && g - s < S && !(g == S - 1 && moved)))
+            b += pair_bound(s, g == S ? S - 1 - s : g - s);
+    }
+    return b;
+}
+__host__ __device__ constexpr int max_group_bound(int S) {
+    int m = 0;
+    for (int g = 0; g <= S; ++g) m = group_bound(S, g) > m ? group_bound(S, g) : m;
+    return m;
+}
+// Longest contraction chunk whose group sums stay exact in FP32 (below 2^24),
+// in k-blocks.
+__host__ __device__ constexpr int chunk_kblocks(int S) { return ((1 << 24) - 1) / max_group_bound(S) / KB; }
+// Groups g and g+1 combine as 128 v_g + v_{g+1} in 32 bits, and group S-1
+// with the extra group as v_{S-1} + v_extra, when that cannot overflow over a
+// whole chunk.
+__host__ __device__ constexpr bool drain_fits_i32(int S) {
+    const double n = chunk_kblocks(S) * KB;
+    bool ok = true;
+    for (int g = 0; g + 1 < S; g += 2)
+        ok = ok && 128.0 * group_bound(S, g) * n + (double)group_bound(S, g + 1) * n < 2147483647.0;
+    return ok && ((double)group_bound(S, S - 1) + group_bound(S, S)) * n < 2147483647.0;
+}
 // Balanced chunking: the fewest exact chunks, of near-equal length.
 inline int64_t balanced_chunk_kb(int64_t Kb, int S) {
     const int64_t n = ceil_div(Kb, chunk_kblocks(S));
     return ceil_div(Kb, std::max<int64_t>(n, 1));
 }
-__host__ __device__ constexpr int tmem_cols(int S) { return S * TN <= 256 ? 256 : 512; }
-
 // Byte offset of element (r, k) inside one [T x 16] operand block: 8-row x
 // 16-byte core matrices, k-adjacent ones 128 B apart (LBO), row groups 256 B
 // apart (SBO).
@@ -510,54 +555,56 @@ __device__ __forceinline__ void add_shifted(int64_t (&acc)[HC], int sh, P p) {
     }
 }
 
-template <int HC>
-__device__ __forceinline__ void add_group(int64_t (&acc)[HC], const uint32_t (&r)[HC], int sh) {
+// acc[j] += v(j) * 2^sh for 32-bit integers v(j); negative shifts round to
+// nearest, ties to even.
+template <int HC, class P>
+__device__ __forceinline__ void add_value(int64_t (&acc)[HC], int sh, P v) {
     if (sh >= 0) {
-        add_shifted<HC>(acc, sh, [&](int j) { return __float2int_rn(__uint_as_float(r[j])); });
+        add_shifted<HC>(acc, sh, v);
     } else {
         const int s = -sh;
         const int64_t half = (1ll << (s - 1)) - 1;
 #pragma unroll
         for (int j = 0; j < HC; ++j) {
-            const int64_t v = (int64_t)__float2int_rn(__uint_as_float(r[j]));
-            acc[j] += (v + half + ((v >> s) & 1)) >> s;
+            const int64_t w = (int64_t)v(j);
+            acc[j] += (w + half + ((w >> s) & 1)) >> s;
         }
     }
 }
 
-// Groups g and g+1 (g+1 < S), or g alone when it is the last.  Where group
-// g+1's shift sh is not negative, (v_g << (sh+7)) + (v_{g+1} << sh) is formed
-// as (128 v_g + v_{g+1}) << sh with the bracket in 32 bits, which is exact: an
-// exact chunk has n <= (2^24 - 1) / (S 65^2) terms, so |v_g| <= (g+1) 65^2 n
-// < (g+1) 2^24 / S and |128 v_g + v_{g+1}| < 2^24 (128 - 127/S) < 2^31.
+__device__ __forceinline__ int32_t f2i(uint32_t bits) { return __float2int_rn(__uint_as_float(bits)); }
+
+// One group, with shift sh.
+template <int HC>
+__device__ __forceinline__ void add_group(int64_t (&acc)[HC], const uint32_t (&r)[HC], int sh) {
+    add_value<HC>(acc, sh, [&](int j) { return f2i(r[j]); });
+}
+
+// Two groups of the same weight (group S-1 and the extra group), with shift sh.
+template <int HC>
+__device__ __forceinline__ void add_group_sum(int64_t (&acc)[HC], const uint32_t (&x)[HC], const uint32_t (&y)[HC],
+                                              int sh) {
+    add_value<HC>(acc, sh, [&](int j) { return f2i(x[j]) + f2i(y[j]); });
+}
+
+// Groups g and g+1 (g+1 < S).  Where group g+1's shift sh is not negative,
+// (v_g << (sh+7)) + (v_{g+1} << sh) is formed as (128 v_g + v_{g+1}) << sh with
+// the bracket in 32 bits, which the chunk length keeps exact (drain_fits_i32).
 template <int S, int HC>
 __device__ __forceinline__ void add_group_pair(int64_t (&acc)[HC], const uint32_t (&x)[HC], const uint32_t (&y)[HC],
                                                int g, int R) {
-    if (g + 1 >= S) {
-        add_group<HC>(acc, x, 7 * (S - 1 - g) - R);
-        return;
-    }
     const int sh = 7 * (S - 2 - g) - R;
     if (sh >= 0) {
-        add_shifted<HC>(acc, sh, [&](int j) {
-            return __float2int_rn(__uint_as_float(x[j])) * 128 + __float2int_rn(__uint_as_float(y[j]));
-        });
+        add_shifted<HC>(acc, sh, [&](int j) { return f2i(x[j]) * 128 + f2i(y[j]); });
     } else {
         add_group<HC>(acc, x, sh + 7);
         add_group<HC>(acc, y, sh);
     }
 }
 
-// Issue the tensor-memory loads of groups g and g+1 (g alone when g+1 == S)
-// for this thread's lane and HC columns starting at col.
+// This thread's lane of HC consecutive TMEM columns.
 __device__ __forceinline__ void tmem_ld_cols(uint32_t taddr, uint32_t (&r)[16]) { ptx::tmem_ld16(taddr, r); }
 __device__ __forceinline__ void tmem_ld_cols(uint32_t taddr, uint32_t (&r)[32]) { ptx::tmem_ld32(taddr, r); }
-
-template <int S, int HC>
-__device__ __forceinline__ void load_group_pair(uint32_t col, int g, uint32_t (&x)[HC], uint32_t (&y)[HC]) {
-    tmem_ld_cols(col + (uint32_t)(g * TN), x);
-    if (g + 1 < S) tmem_ld_cols(col + (uint32_t)((g + 1) * TN), y);
-}
 
 __device__ __forceinline__ int64_t out_addr(const OutMap& o, int64_t m, int64_t n) {
     return (m % o.md) * o.ms0 + (m / o.md) * o.ms1 + (n % o.nd) * o.ns0 + (n / o.nd) * o.ns1;
@@ -775,13 +822,17 @@ __global__ void __launch_bounds__(FUSED ? NTHREADS_FUSED : NTHREADS, 1)
                         // shared memory and form one K-major operand of 64*(S-s) rows; their
                         // products land in adjacent accumulator groups s .. S-1.  One MMA with
                         // N = 64*(S-s) (split at 256) therefore covers all pairs of digit s.
+                        // A lone product of the last group with s >= 1 goes to the extra group
+                        // (column block S), which the first of them starts on a chunk's first k-step.
 #pragma unroll
                         for (int s = 0; s < S; ++s) {
 #pragma unroll
                             for (int t0 = 0; t0 < S - s; t0 += 4) {
                                 const int nt = (S - s - t0) < 4 ? (S - s - t0) : 4;
-                                const uint32_t acc = (first && s == 0) ? 0u : 1u;
-                                ptx::mma_bf16_ss(tmem + (uint32_t)((s + t0) * TN), adesc0 + soff + (uint64_t)((s * A_BLK) >> 4),
+                                const bool xg = extra_pair(S, s) && t0 + 1 == S - s;
+                                const uint32_t acc = (first && s == (xg ? first_extra_pair(S) : 0)) ? 0u : 1u;
+                                ptx::mma_bf16_ss(tmem + (uint32_t)((xg ? S : s + t0) * TN),
+                                                 adesc0 + soff + (uint64_t)((s * A_BLK) >> 4),
                                                  bdesc0 + soff + (uint64_t)((t0 * B_BLK) >> 4),
                                                  ptx::idesc_bf16_f32(TM, TN * nt), acc);
                             }
@@ -865,38 +916,56 @@ __global__ void __launch_bounds__(FUSED ? NTHREADS_FUSED : NTHREADS, 1)
             for (int64_t c = c0; c < c1; ++c, ++cc) {
                 if (!ptx::mbar_wait(acc_full, (uint32_t)(cc & 1), a.err)) { ok = false; break; }
                 ptx::tc_fence_after();
-                // Groups are read in pairs (one per load round with 16 columns per
-                // thread; single groups with 32, for registers).  The tensor memory is
-                // handed back to the MMA warp as soon as the last load has landed, before
-                // the last conversion.
+                // Groups are read in pairs, one load round each (with 16 columns per
+                // thread; one group per round with 32, for registers): (0,1), (2,3), ...,
+                // and group S-1 with the extra group.  The tensor memory is handed back
+                // to the MMA warp as soon as the last round's loads have landed, before
+                // its conversion.
                 const uint32_t col = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(h * HC);
+                auto release = [&]() {
+                    ptx::tc_fence_before();
+                    ptx::mbar_arrive(acc_empty);
+                };
+                const int sh_last = -a.R;  // shift of group S-1 (and of the extra group)
                 uint32_t x[HC];
                 if constexpr (HC <= 16) {
+                    static_assert(drain_fits_i32(S), "paired drain would overflow 32 bits");
                     uint32_t y[HC];
+                    // Rounds: pairs (g, g+1) for even g < S-1; then, for odd S, group S-1
+                    // (with the extra group); for even S with an extra group, that alone.
+                    constexpr int ROUNDS = (S + 1) / 2 + ((S % 2 == 0 && extra_group(S)) ? 1 : 0);
 #pragma unroll 1
-                    for (int g = 0;; g += 2) {
-                        load_group_pair<S, HC>(col, g, x, y);
-                        ptx::tmem_wait_ld();
-                        const bool last = g + 2 >= S;
-                        if (last) {
-                            ptx::tc_fence_before();
-                            ptx::mbar_arrive(acc_empty);
+                    for (int u = 0; u < ROUNDS; ++u) {
+                        const int g = 2 * u;
+                        const bool last = u + 1 == ROUNDS;
+                        if (g + 1 < S) {
+                            tmem_ld_cols(col + (uint32_t)(g * TN), x);
+                            tmem_ld_cols(col + (uint32_t)((g + 1) * TN), y);
+                            ptx::tmem_wait_ld();
+                            if (last) release();
+                            add_group_pair<S, HC>(acc, x, y, g, a.R);
+                        } else if (g == S - 1) {
+                            tmem_ld_cols(col + (uint32_t)(g * TN), x);
+                            if constexpr (extra_group(S)) tmem_ld_cols(col + (uint32_t)(S * TN), y);
+                            ptx::tmem_wait_ld();
+                            if (last) release();
+                            if constexpr (extra_group(S)) add_group_sum<HC>(acc, x, y, sh_last);
+                            else add_group<HC>(acc, x, sh_last);
+                        } else {
+                            tmem_ld_cols(col + (uint32_t)(S * TN), x);
+                            ptx::tmem_wait_ld();
+                            if (last) release();
+                            add_group<HC>(acc, x, sh_last);
                         }
-                        add_group_pair<S, HC>(acc, x, y, g, a.R);
-                        if (last) break;
                     }
                 } else {
+                    constexpr int ROUNDS = S + (extra_group(S) ? 1 : 0);
 #pragma unroll 1
-                    for (int g = 0;; ++g) {
+                    for (int g = 0; g < ROUNDS; ++g) {
                         tmem_ld_cols(col + (uint32_t)(g * TN), x);
                         ptx::tmem_wait_ld();
-                        const bool last = g + 1 >= S;
-                        if (last) {
-                            ptx::tc_fence_before();
-                            ptx::mbar_arrive(acc_empty);
-                        }
-                        add_group<HC>(acc, x, 7 * (S - 1 - g) - a.R);
-                        if (last) break;
+                        if (g + 1 == ROUNDS) release();
+                        add_group<HC>(acc, x, g < S ? 7 * (S - 1 - g) - a.R : sh_last);
                     }
                 }
             }

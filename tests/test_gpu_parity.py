@@ -137,12 +137,14 @@ def test_ri_ov_k_split_matches_oracle(nb, naux, nocc):
     assert np.array_equal(Kh, Kh.T)
 
 
-def test_split_multichunk_contraction():
-    # nb > 640 forces two exact chunks along the contraction in the first half-transform.
-    nb, naux, nocc = 700, 3, 6
+@pytest.mark.parametrize("S,nb", [(6, 850), (7, 700)])
+def test_split_multichunk_contraction(S, nb):
+    # nb above the exact-chunk length (800 terms at S = 6, 672 at S = 7) forces two
+    # exact chunks along the contraction in the first half-transform.
+    naux, nocc = 3, 6
     C, B = inputs(nb, naux, seed=11)
     ov_ref, K_ref = oracle.ri_ov_k(C, B, nocc)
-    ov, K = rt.ri_ov_k(dev(C), dev(B), nb, naux, nocc, nb - nocc, form="split", nslices=6)
+    ov, K = rt.ri_ov_k(dev(C), dev(B), nb, naux, nocc, nb - nocc, form="split", nslices=S)
     assert np.max(np.abs(host(ov, (nocc, nb - nocc, naux)) - ov_ref)) < 1e-10
     assert relerr(host(K, (nb, nb)), K_ref) < 1e-11
 
