@@ -39,6 +39,10 @@ FLOPS = NAUX * FLOPS_PER_SLAB  # 3.007e11
 
 
 FALLBACK_PEAKS = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}
+# float64 FMA rate of a GB300, from a DFMA throughput probe of this repository
+# (register-resident chains, all SMs); used as RI-J's roofline.
+DFMA_TFLOPS = 1.20
+DFMA_SOURCE = "DFMA throughput probe on GB300 (1.20 TFLOP/s); MEASURED_PEAKS.json holds no float64 rate"
 
 
 def workload():
@@ -996,11 +1000,37 @@ def main():
     rij_bytes = 2.0 * 8 * NB * NB * NAUX + 8.0 * 3 * NB * NB
     one_read = 8.0 * NB * NB * NAUX + 8.0 * 2 * NB * NB
     hbm = peaks()[0].get("hbm_gbs", FALLBACK_PEAKS["hbm_gbs"])
+    # Both passes do one float64 FMA per element of ri3ao: the DFMA rate bounds them.
+    rij_flop = 2.0 * 2 * NB * NB * NAUX
     rij = {"ms": rij_ms, "achieved_gbs": rij_bytes / rij_ms / 1e6, "peak_gbs": hbm,
            "frac": rij_bytes / rij_ms / 1e6 / hbm, "bytes": rij_bytes,
            "frac_vs_one_read": one_read / rij_ms / 1e6 / hbm, "one_read_bytes": one_read,
+           "dfma": {"bound": "dfma", "flop": rij_flop, "achieved_tflops": rij_flop / rij_ms / 1e9,
+                    "peak_tflops": DFMA_TFLOPS, "frac": rij_flop / rij_ms / 1e9 / DFMA_TFLOPS,
+                    "peak_source": DFMA_SOURCE},
            "kernels": "rij_w_kernel + rij_j_kernel (float64, two streaming reads of ri3ao)"}
-    del w_j, J_j
+    # The same on symmetric slabs (rt_ri_j_symmetric): upper triangles only, each product once.
+    w_s = torch.empty(NAUX, dtype=torch.float64, device=dev)
+    J_s = torch.empty(NB * NB, dtype=torch.float64, device=dev)
+    for _ in range(3):
+        rt.ri_j(B, D, NB, NAUX, w=w_s, J=J_s, stream=stream, symmetric=True)
+    barrier()
+    e0.record(stream)
+    for _ in range(10):
+        rt.ri_j(B, D, NB, NAUX, w=w_s, J=J_s, stream=stream, symmetric=True)
+    e1.record(stream)
+    barrier()
+    sym_ms = e0.elapsed_time(e1) / 10
+    tri = NB * (NB + 1) / 2.0
+    sym_flop, sym_bytes = 2.0 * 2 * tri * NAUX, 2.0 * 8 * tri * NAUX
+    rij["symmetric"] = {
+        "ms": sym_ms, "speedup_vs_full": rij_ms / sym_ms,
+        "achieved_tflops": sym_flop / sym_ms / 1e9, "dfma_frac": sym_flop / sym_ms / 1e9 / DFMA_TFLOPS,
+        "achieved_gbs": sym_bytes / sym_ms / 1e6, "hbm_frac": sym_bytes / sym_ms / 1e6 / hbm,
+        "w_max_rel_vs_full": float((w_s - w_j).abs().max() / w_j.abs().max()),
+        "J_max_rel_vs_full": float((J_s - J_j).abs().max() / J_j.abs().max()),
+        "kernels": "rij_w_sym_kernel + rij_j_sym_kernel + rij_j_sym_finish (upper triangles of ri3ao and D)"}
+    del w_j, J_j, w_s, J_s
 
     # ---- end to end through the host-pointer C ABI (pinned host buffers)
     e2e = e2e_full = None

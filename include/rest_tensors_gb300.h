@@ -226,6 +226,15 @@ rt_status rt_ri_ov_k_batched(const rt_ri_problem* probs, int nprob, int form, in
  * ri.rs:309-316) and J = sum_P w[P] B^P.  w may be NULL. */
 rt_status rt_ri_j(const double* B, const double* D, int nb, int naux, double* w, double* J, void* stream);
 
+/* rt_ri_j for symmetric slabs and a symmetric D, the case of (mu nu|P) and of
+ * a density matrix: reads only the entries mu <= nu of every B^P and of D (the
+ * rest may hold anything) and forms each product once, w[P] as
+ * sum_{mu<=nu} (2 - delta_{mu nu}) D[mu,nu] B^P[mu,nu] and J's upper triangle,
+ * which it mirrors.  Both passes are bound by the float64 FMA rate, so this
+ * takes about half the time of rt_ri_j.  No counterpart in the reference (its
+ * ri3fn has the same symmetry; rt_ri_j follows its full contraction). */
+rt_status rt_ri_j_symmetric(const double* B, const double* D, int nb, int naux, double* w, double* J, void* stream);
+
 /* Exchange energy E_x = -tr(D K) = -sum_{mu,nu} D[mu,nu] K[mu,nu], reduced in
  * float64 with a fixed-order tree.  Writes one double to ex_device. */
 rt_status rt_ri_exchange_energy(const double* D, const double* K, int nb, double* ex_device, void* stream);

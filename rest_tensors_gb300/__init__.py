@@ -113,6 +113,8 @@ def lib() -> ctypes.CDLL:
     L.rt_ri3ao_release.argtypes = [vp]
     L.rt_ri_j.restype = c_int
     L.rt_ri_j.argtypes = [vp, vp, c_int, c_int, vp, vp, vp]
+    L.rt_ri_j_symmetric.restype = c_int
+    L.rt_ri_j_symmetric.argtypes = [vp, vp, c_int, c_int, vp, vp, vp]
     L.rt_ri_exchange_energy.restype = c_int
     L.rt_ri_exchange_energy.argtypes = [vp, vp, c_int, vp, vp]
     L.rt_synth_ri3ao.restype = c_int
@@ -655,15 +657,18 @@ def dspgvx(ap, bp, n: int, num_orb: int, eigvec=None, w=None, form: str = "fp64"
     return eigvec, w
 
 
-def ri_j(B, D, nb: int, naux: int, w=None, J=None, stream=None):
+def ri_j(B, D, nb: int, naux: int, w=None, J=None, stream=None, symmetric: bool = False):
+    """RI-J (w, J).  symmetric=True calls rt_ri_j_symmetric: every slab of B and
+    D must be symmetric; only their entries mu <= nu are read."""
     import torch
 
     if w is None:
         w = torch.empty(naux, dtype=torch.float64, device=B.device)
     if J is None:
         J = torch.empty(nb * nb, dtype=torch.float64, device=B.device)
-    _check(lib().rt_ri_j(_dptr(B, nb * nb * naux, "B"), _dptr(D, nb * nb, "D"), nb, naux, _dptr(w, naux, "w"),
-                         _dptr(J, nb * nb, "J"), _stream(stream)))
+    fn = lib().rt_ri_j_symmetric if symmetric else lib().rt_ri_j
+    _check(fn(_dptr(B, nb * nb * naux, "B"), _dptr(D, nb * nb, "D"), nb, naux, _dptr(w, naux, "w"),
+              _dptr(J, nb * nb, "J"), _stream(stream)))
     return w, J
 
 

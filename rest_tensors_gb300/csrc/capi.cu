@@ -15,6 +15,8 @@ namespace rt {
 
 
 rt_status ri_j_fp64(const double* B, const double* D, int nb, int naux, double* w, double* J, cudaStream_t stream);
+rt_status ri_j_fp64_symmetric(const double* B, const double* D, int nb, int naux, double* w, double* J,
+                              cudaStream_t stream);
 rt_status exchange_energy(const double* D, const double* K, int nb, double* out, cudaStream_t stream);
 rt_status synth_ri3ao(uint64_t seed, int nb, int P0, int nslab, double* B, cudaStream_t stream);
 rt_status synth_coef_seed(uint64_t seed, int nb, double* M, cudaStream_t stream);
@@ -626,6 +628,22 @@ rt_status rt_ri_j(const double* B, const double* D, int nb, int naux, double* w,
     }
     RT_REQUIRE(B && D, "rt_ri_j: null input pointer");
     return ri_j_fp64(B, D, nb, naux, w, J, s);
+}
+
+rt_status rt_ri_j_symmetric(const double* B, const double* D, int nb, int naux, double* w, double* J, void* stream) {
+    NvtxRange nvtx_range("rt_ri_j_symmetric");
+    RT_REQUIRE(nb >= 0 && naux >= 0, "rt_ri_j_symmetric: negative dimension");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (naux == 0) {
+        if (J && nb) RT_CUDA_TRY(cudaMemsetAsync(J, 0, sizeof(double) * nb * (size_t)nb, s));
+        return RT_OK;
+    }
+    if (nb == 0) {
+        if (w) RT_CUDA_TRY(cudaMemsetAsync(w, 0, sizeof(double) * naux, s));
+        return RT_OK;
+    }
+    RT_REQUIRE(B && D, "rt_ri_j_symmetric: null input pointer");
+    return ri_j_fp64_symmetric(B, D, nb, naux, w, J, s);
 }
 
 rt_status rt_ri_exchange_energy(const double* D, const double* K, int nb, double* ex_device, void* stream) {

@@ -534,6 +534,142 @@ __global__ void synth_coef_kernel(uint64_t seed, int nb, double* M) {
         M[idx] = rt_coef_seed_elem(seed, idx % nb, idx / nb);
 }
 
+// ---- RI-J on symmetric slabs (B^P and D symmetric): only entries mu <= nu
+// are read, and each product is formed once.  Both passes are bound by the
+// float64 FMA rate, so halving the products halves the time.
+
+// D2[mu, nu] = 2 D[mu, nu] above the diagonal, D[mu, mu] on it, 0 below:
+// w_P = sum_{mu <= nu} D2[mu, nu] B^P[mu, nu].
+__global__ void rij_d2_kernel(const double* __restrict__ D, int nb, double* __restrict__ D2) {
+    const int64_t n2 = (int64_t)nb * nb;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n2; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t mu = e % nb, nu = e / nb;
+        D2[e] = mu < nu ? 2.0 * D[e] : (mu == nu ? D[e] : 0.0);
+    }
+}
+
+// w[P] for slab P, one block per slab: warp c takes the column pairs
+// (c, nb-1-c), (c+8, nb-9-c), ... (nb+1 upper entries per pair), lanes run down
+// each column's upper part with four loads in flight; fixed-order reduction.
+__global__ void __launch_bounds__(256) rij_w_sym_kernel(const double* __restrict__ B, const double* __restrict__ D2,
+                                                        int nb, int naux, double* __restrict__ w) {
+    __shared__ double red[8];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t n2 = (int64_t)nb * nb;
+    const int half = (nb + 1) / 2;
+    for (int P = blockIdx.x; P < naux; P += gridDim.x) {
+        const double* b = B + (int64_t)P * n2;
+        double s[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int c = warp; c < half; c += 8) {
+#pragma unroll 1
+            for (int side = 0; side < 2; ++side) {
+                const int nu = side ? nb - 1 - c : c;
+                if (side && nu == c) break;
+                const double* bc = b + (int64_t)nb * nu;
+                const double* dc = D2 + (int64_t)nb * nu;
+                int mu = lane;
+                for (; mu + 96 <= nu; mu += 128) {
+                    double x[4], y[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        x[u] = bc[mu + 32 * u];
+                        y[u] = dc[mu + 32 * u];
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) s[u] = fma(x[u], y[u], s[u]);
+                }
+                for (; mu <= nu; mu += 32) s[0] = fma(bc[mu], dc[mu], s[0]);
+            }
+        }
+        double t0 = (s[0] + s[1]) + (s[2] + s[3]);
+        for (int o = 16; o > 0; o >>= 1) t0 += __shfl_xor_sync(0xffffffffu, t0, o);
+        if (lane == 0) red[warp] = t0;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            double t = threadIdx.x < 8 ? red[threadIdx.x] : 0.0;
+            for (int o = 4; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+            if (threadIdx.x == 0) w[P] = t;
+        }
+        __syncthreads();
+    }
+}
+
+// Column nu and row mu of packed upper-triangle index t = nu (nu + 1) / 2 + mu.
+__device__ __forceinline__ void tri_index(int64_t t, int& mu, int& nu) {
+    int64_t v = (int64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    while (v * (v + 1) / 2 > t) --v;
+    while ((v + 1) * (v + 2) / 2 <= t) ++v;
+    nu = (int)v;
+    mu = (int)(t - v * (v + 1) / 2);
+}
+
+// Partial J over the slab range of split blockIdx.y: each thread owns packed
+// upper-triangle entries t and t+1, part[split][t] = sum_P w[P] B^P[mu, nu].
+__global__ void __launch_bounds__(256) rij_j_sym_kernel(const double* __restrict__ B, const double* __restrict__ w,
+                                                        int nb, int naux, int64_t T, int pspan,
+                                                        double* __restrict__ part) {
+    __shared__ double ws[1024];
+    const int64_t n2 = (int64_t)nb * nb;
+    const int64_t t0 = 2 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+    const bool v0 = t0 < T, v1 = t0 + 1 < T;
+    int mu, nu;
+    int64_t o0 = 0, o1 = 0;
+    if (v0) {
+        tri_index(t0, mu, nu);
+        o0 = mu + (int64_t)nb * nu;
+    }
+    if (v1) {
+        tri_index(t0 + 1, mu, nu);
+        o1 = mu + (int64_t)nb * nu;
+    }
+    const int Pb = blockIdx.y * pspan, Pe = min(naux, Pb + pspan);
+    double a0 = 0.0, a1 = 0.0, c0 = 0.0, c1 = 0.0;
+    for (int P0 = Pb; P0 < Pe; P0 += 1024) {
+        const int np = min(1024, Pe - P0);
+        __syncthreads();
+        for (int t = threadIdx.x; t < np; t += blockDim.x) ws[t] = w[P0 + t];
+        __syncthreads();
+        if (!v0) continue;
+        const double* b0 = B + o0 + (int64_t)P0 * n2;
+        const double* b1 = B + (v1 ? o1 : o0) + (int64_t)P0 * n2;
+        int p = 0;
+        for (; p + 3 < np; p += 4) {
+            double x[4], y[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                x[u] = b0[(int64_t)(p + u) * n2];
+                y[u] = b1[(int64_t)(p + u) * n2];
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u += 2) {
+                a0 = fma(ws[p + u], x[u], a0);
+                a1 = fma(ws[p + u], y[u], a1);
+                c0 = fma(ws[p + u + 1], x[u + 1], c0);
+                c1 = fma(ws[p + u + 1], y[u + 1], c1);
+            }
+        }
+        for (; p < np; ++p) {
+            a0 = fma(ws[p], b0[(int64_t)p * n2], a0);
+            a1 = fma(ws[p], b1[(int64_t)p * n2], a1);
+        }
+    }
+    if (v0) part[(int64_t)blockIdx.y * T + t0] = a0 + c0;
+    if (v1) part[(int64_t)blockIdx.y * T + t0 + 1] = a1 + c1;
+}
+
+// J[mu, nu] = J[nu, mu] = the splits' partials summed in order.
+__global__ void rij_j_sym_finish(const double* __restrict__ part, int nb, int64_t T, int splits,
+                                 double* __restrict__ J) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < T; t += (int64_t)gridDim.x * blockDim.x) {
+        double a = 0.0;
+        for (int z = 0; z < splits; ++z) a += part[(int64_t)z * T + t];
+        int mu, nu;
+        tri_index(t, mu, nu);
+        J[mu + (int64_t)nb * nu] = a;
+        J[nu + (int64_t)nb * mu] = a;
+    }
+}
+
 __global__ void synth_kernel(uint64_t seed, int nb, int P0, int64_t total, double* B) {
     const int64_t nb2 = (int64_t)nb * nb;
     for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
@@ -564,6 +700,36 @@ rt_status ri_j_fp64(const double* B, const double* D, int nb, int naux, double* 
             rij_j_kernel_scalar<<<(unsigned)ceil_div(n2, 256), 256, 0, stream>>>(B, w, n2, naux, J);
         }
         RT_TRY(check_launch("rij_j_kernel"));
+    }
+    return RT_OK;
+}
+
+rt_status ri_j_fp64_symmetric(const double* B, const double* D, int nb, int naux, double* w, double* J,
+                              cudaStream_t stream) {
+    const int64_t n2 = (int64_t)nb * nb, T = (int64_t)nb * (nb + 1) / 2;
+    ScratchBuf wbuf, d2buf, partbuf;
+    if (!w) {
+        RT_TRY(scratch_alloc(wbuf, sizeof(double) * (size_t)naux, stream));
+        w = wbuf.as<double>();
+    }
+    RT_TRY(scratch_alloc(d2buf, sizeof(double) * (size_t)n2, stream));
+    double* D2 = d2buf.as<double>();
+    rij_d2_kernel<<<(unsigned)std::min<int64_t>(ceil_div(n2, 256), 4 * sm_count()), 256, 0, stream>>>(D, nb, D2);
+    RT_TRY(check_launch("rij_d2_kernel"));
+    rij_w_sym_kernel<<<(unsigned)naux, 256, 0, stream>>>(B, D2, nb, naux, w);
+    RT_TRY(check_launch("rij_w_sym_kernel"));
+    if (J) {
+        // Split the slabs so that about eight blocks per SM run the J pass.
+        const int64_t bx = ceil_div(ceil_div(T, (int64_t)2), (int64_t)256);
+        const int splits = (int)std::max<int64_t>(1, std::min<int64_t>({ceil_div(8 * (int64_t)sm_count(), bx), 16, naux}));
+        const int pspan = (int)ceil_div((int64_t)naux, (int64_t)splits);
+        RT_TRY(scratch_alloc(partbuf, sizeof(double) * (size_t)(splits * T), stream));
+        double* part = partbuf.as<double>();
+        rij_j_sym_kernel<<<dim3((unsigned)bx, (unsigned)splits), 256, 0, stream>>>(B, w, nb, naux, T, pspan, part);
+        RT_TRY(check_launch("rij_j_sym_kernel"));
+        rij_j_sym_finish<<<(unsigned)std::min<int64_t>(ceil_div(T, 256), 4 * sm_count()), 256, 0, stream>>>(
+            part, nb, T, splits, J);
+        RT_TRY(check_launch("rij_j_sym_finish"));
     }
     return RT_OK;
 }

@@ -192,6 +192,37 @@ def test_ri_j_matches_oracle(nb, naux):
     assert torch.equal(w, w2) and torch.equal(J, J2)
 
 
+# The synthetic ri3ao is symmetric per slab; odd and even nb, one column pair
+# per warp and many, naux above one 1024-slab w stage and split over blocks.
+@pytest.mark.parametrize("nb,naux", [(1, 3), (2, 5), (20, 12), (33, 7), (100, 400), (40, 1100), (600, 96), (751, 33)])
+def test_ri_j_symmetric_matches_oracle(nb, naux):
+    C, B = inputs(nb, naux, seed=1)
+    D = np.asfortranarray(C[:, :5] @ C[:, :5].T)
+    D = np.asfortranarray(0.5 * (D + D.T))
+    w_ref, J_ref = oracle.ri_j(B, D)
+    w, J = rt.ri_j(dev(B), dev(D), nb, naux, symmetric=True)
+    assert relerr(w.cpu().numpy(), w_ref) < 1e-12
+    Jh = host(J, (nb, nb))
+    assert relerr(Jh, J_ref) < 1e-12
+    assert np.array_equal(Jh, Jh.T)
+    w2, J2 = rt.ri_j(dev(B), dev(D), nb, naux, symmetric=True)
+    assert torch.equal(w, w2) and torch.equal(J, J2)
+
+
+def test_ri_j_symmetric_reads_only_the_upper_triangles():
+    nb, naux = 90, 70
+    C, B = inputs(nb, naux, seed=2)
+    D = np.asfortranarray(C[:, :7] @ C[:, :7].T)
+    D = np.asfortranarray(0.5 * (D + D.T))
+    w_ref, J_ref = rt.ri_j(dev(B), dev(D), nb, naux, symmetric=True)
+    low = np.tril(np.ones((nb, nb), dtype=bool), -1)
+    Bg, Dg = B.copy(order="F"), D.copy(order="F")
+    Bg[low, :] = 1e300  # anything below the diagonal must be ignored
+    Dg[low] = -1e300
+    w, J = rt.ri_j(dev(Bg), dev(Dg), nb, naux, symmetric=True)
+    assert torch.equal(w, w_ref) and torch.equal(J, J_ref)
+
+
 @pytest.mark.parametrize("form", ["fp64", "split"])
 def test_exchange_energy(form):
     nb, naux, nocc = 100, 400, 20
