@@ -183,11 +183,11 @@ __global__ void emax_contig_kernel(Operand a, int64_t K, int* __restrict__ emax,
 
 // Same for rows whose consecutive r are contiguous (s0 == 1): thread per row,
 // blockIdx.y splits k; results combine through atomicMax on a zeroed array.
-__global__ void emax_strided_kernel(Operand a, int64_t K, int64_t kspan, int* __restrict__ emax,
-                                    unsigned int* err) {
-    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void emax_strided_body(const Operand& a, int64_t K, int64_t kspan, int* __restrict__ emax,
+                                                  unsigned int* err, int64_t bx, int64_t by) {
+    const int64_t r = bx * blockDim.x + threadIdx.x;
     if (r >= a.rows) return;
-    const int64_t k0 = (int64_t)blockIdx.y * kspan, k1 = min(K, k0 + kspan);
+    const int64_t k0 = by * kspan, k1 = min(K, k0 + kspan);
     const double* base = a.p + (r % a.div) * a.s0 + (r / a.div) * a.s1;
     unsigned int m = 0;  // maximum of the sign-cleared high words
     const double* src = base + k0 * a.sk;
@@ -195,6 +195,10 @@ __global__ void emax_strided_kernel(Operand a, int64_t K, int64_t kspan, int* __
     m >>= 20;
     if (m == 0x7FFu) atomicOr(err, DEV_ERR_NONFINITE);
     if (m) atomicMax(&emax[r], (int)m);
+}
+__global__ void emax_strided_kernel(Operand a, int64_t K, int64_t kspan, int* __restrict__ emax,
+                                    unsigned int* err) {
+    emax_strided_body(a, K, kspan, emax, err, blockIdx.x, blockIdx.y);
 }
 
 // --------------------------------------------------------------- slicing --
@@ -266,10 +270,8 @@ __device__ __forceinline__ void store8(const SliceArgs& a, int64_t tile, int64_t
 // Strided rows (s0 == 1): CTA = (tile, 32 k); work item = (row, 8 consecutive
 // k), rows fastest, so reads are coalesced across consecutive rows.
 template <int S>
-__global__ void __launch_bounds__(256) slice_strided_kernel(SliceArgs a) {
+__device__ __forceinline__ void slice_strided_body(const SliceArgs& a, int64_t tile, int64_t k32) {
     const int T = a.T;
-    const int64_t tile = blockIdx.x;
-    const int64_t k32 = blockIdx.y;
     for (int item = threadIdx.x; item < T * (SK / 8); item += blockDim.x) {
         const int r = item % T, q = item / T;
         const int64_t kb = k32 * (SK / KB) + (q >> 1);
@@ -292,6 +294,10 @@ __global__ void __launch_bounds__(256) slice_strided_kernel(SliceArgs a) {
         digits8<S>(x, em, w);
         store8<S>(a, tile, kb, r, (q & 1) * 8, w);
     }
+}
+template <int S>
+__global__ void __launch_bounds__(256) slice_strided_kernel(SliceArgs a) {
+    slice_strided_body<S>(a, blockIdx.x, blockIdx.y);
 }
 
 // Strided rows (s0 == 1) with a short contraction (K <= 8 * (256 / RR) * NBLK):
@@ -450,6 +456,23 @@ template <int S, int NBLK>
 __global__ void __launch_bounds__(256, 2) slice_contig_rowmax_grouped(const __grid_constant__ SliceGroup G) {
     const int p = slice_job(G, blockIdx.x);
     slice_contig_rowmax_body<S, NBLK>(G.a[p], G.emax[p], (int64_t)blockIdx.x - G.prefix[p]);
+}
+
+// Long contractions over strided rows, two passes for many operands at once:
+// job p's blocks are its 2-D grid flattened, x fastest.
+constexpr int64_t kStridedSpan = 512;  // k per row-exponent block
+__global__ void __launch_bounds__(256) emax_strided_grouped(const __grid_constant__ SliceGroup G) {
+    const int p = slice_job(G, blockIdx.x);
+    const SliceArgs& a = G.a[p];
+    const int64_t b = (int64_t)blockIdx.x - G.prefix[p], gx = (a.src.rows + 255) / 256;
+    emax_strided_body(a.src, a.K, kStridedSpan, G.emax[p], a.err, b % gx, b / gx);
+}
+template <int S>
+__global__ void __launch_bounds__(256) slice_strided_grouped(const __grid_constant__ SliceGroup G) {
+    const int p = slice_job(G, blockIdx.x);
+    const SliceArgs& a = G.a[p];
+    const int64_t b = (int64_t)blockIdx.x - G.prefix[p];
+    slice_strided_body<S>(a, b % a.tiles, b / a.tiles);
 }
 
 // Contiguous rows (sk == 1): the [T x 32] tile is staged through shared
@@ -1013,27 +1036,48 @@ __device__ __forceinline__ double scale_pow2_i128(__int128 v, int ex) {
 
 // Sum split-K int64 partials exactly in 128 bits and round once to float64.
 template <int S>
-__global__ void oz_finalize_kernel(GemmArgs a) {
+__device__ __forceinline__ void finalize_elem(const GemmArgs& a, int64_t idx) {
     const int64_t ldp = a.tiles_n * TN;
+    const int64_t n = idx / a.M, m = idx % a.M;
+    if (a.symmetric && n < m) return;
+    __int128 v = 0;
+    for (int z = 0; z < a.splits; ++z) v += (__int128)a.partial[((int64_t)z * a.tiles_m * TM + m) * ldp + n];
+    const int ex = a.ea[m] + a.eb[n] - 2056 - 7 * (S - 1) + a.R;
+    a.out.p[out_addr(a.out, m, n)] = scale_pow2_i128(v, ex);
+}
+template <int S>
+__global__ void oz_finalize_kernel(GemmArgs a) {
     const int64_t total = a.M * a.N;
     for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
-         idx += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t n = idx / a.M, m = idx % a.M;
-        if (a.symmetric && n < m) continue;
-        __int128 v = 0;
-        for (int z = 0; z < a.splits; ++z) v += (__int128)a.partial[((int64_t)z * a.tiles_m * TM + m) * ldp + n];
-        const int ex = a.ea[m] + a.eb[n] - 2056 - 7 * (S - 1) + a.R;
-        a.out.p[out_addr(a.out, m, n)] = scale_pow2_i128(v, ex);
-    }
+         idx += (int64_t)gridDim.x * blockDim.x)
+        finalize_elem<S>(a, idx);
 }
 
 // C(m, n) = C(n, m) for m > n (the symmetric product computes n >= m).
+__device__ __forceinline__ void mirror_elem(const OutMap& o, int64_t N, int64_t idx) {
+    const int64_t m = idx % N, n = idx / N;
+    if (m > n) o.p[out_addr(o, m, n)] = o.p[out_addr(o, n, m)];
+}
 __global__ void mirror_kernel(OutMap o, int64_t N) {
     const int64_t total = N * N;
     for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
-         idx += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t m = idx % N, n = idx / N;
-        if (m > n) o.p[out_addr(o, m, n)] = o.p[out_addr(o, n, m)];
+         idx += (int64_t)gridDim.x * blockDim.x)
+        mirror_elem(o, N, idx);
+}
+
+// The same for many products in one launch: block b does 1024 output elements
+// of the product whose range of blocks (prefix) holds b.
+constexpr int64_t kFinishBlock = 1024;
+template <int S, int MAXG, bool MIRROR>
+__global__ void __launch_bounds__(256) finish_grouped(const __grid_constant__ GroupArgs<MAXG> G) {
+    int p = 0;
+    while (p + 1 < G.n && (int64_t)blockIdx.x >= G.prefix[p + 1]) ++p;
+    const GemmArgs& a = G.a[p];
+    const int64_t e0 = ((int64_t)blockIdx.x - G.prefix[p]) * kFinishBlock;
+    const int64_t e1 = min(e0 + kFinishBlock, a.M * a.N);
+    for (int64_t idx = e0 + threadIdx.x; idx < e1; idx += blockDim.x) {
+        if (MIRROR) mirror_elem(a.out, a.M, idx);
+        else finalize_elem<S>(a, idx);
     }
 }
 
@@ -1080,7 +1124,7 @@ rt_status row_exponents(const Operand& op, int64_t K, int* emax, cudaStream_t st
 
 // One-pass slicing jobs collected by the grouped path and launched together.
 struct SliceJob {
-    int kind;   // 0: contiguous rows, 1: strided rows
+    int kind;   // 0: contiguous rows, 1: strided rows, 2 / 3: row exponents / digits of long strided rows
     int nblk;   // the kernel's NBLK
     SliceArgs sa;
     int* emax;
@@ -1093,6 +1137,14 @@ struct SliceQueue {
 template <int S>
 rt_status launch_slice_group(int kind, int nblk, const SliceGroup& G, unsigned grid, cudaStream_t stream) {
     constexpr int RR = kStridedRows, KQN = 256 / RR;
+    if (kind == 2) {
+        emax_strided_grouped<<<grid, 256, 0, stream>>>(G);
+        return check_launch("emax_strided_grouped");
+    }
+    if (kind == 3) {
+        slice_strided_grouped<S><<<grid, 256, 0, stream>>>(G);
+        return check_launch("slice_strided_grouped");
+    }
     if (kind == 0) {
         switch (nblk) {
             case 1: slice_contig_rowmax_grouped<S, 1><<<grid, 256, 0, stream>>>(G); break;
@@ -1115,10 +1167,15 @@ rt_status launch_slice_group(int kind, int nblk, const SliceGroup& G, unsigned g
 }
 
 // Launch the queued jobs: one grouped launch per (kind, NBLK) and per 48 jobs.
+// Row exponents of long strided rows (kind 2) all go before their digits (kind 3).
 template <int S>
 rt_status flush_slices(SliceQueue& q, cudaStream_t stream) {
     std::vector<bool> done(q.jobs.size(), false);
-    for (size_t i = 0; i < q.jobs.size(); ++i) {
+    std::vector<size_t> order;
+    for (int pass = 0; pass < 2; ++pass)
+        for (size_t i = 0; i < q.jobs.size(); ++i)
+            if ((q.jobs[i].kind == 3) == (pass == 1)) order.push_back(i);
+    for (size_t i : order) {
         if (done[i]) continue;
         const int kind = q.jobs[i].kind, nblk = q.jobs[i].nblk;
         SliceGroup G{};
@@ -1223,7 +1280,12 @@ rt_status slice_operand(const Operand& op, int64_t K, int T, Sliced& out, cudaSt
         RT_TRY(check_launch("slice_strided_rowmax_kernel"));
     } else if (op.s0 == 1) {
         RT_CUDA_TRY(cudaMemsetAsync(out.em, 0, sizeof(int) * (size_t)op.rows, stream));
-        const int64_t kspan = 512;
+        if (queue) {
+            queue->jobs.push_back(SliceJob{2, 0, sa, out.em, ceil_div(op.rows, (int64_t)256) * ceil_div(K, kStridedSpan)});
+            queue->jobs.push_back(SliceJob{3, 0, sa, out.em, out.tiles * ceil_div(K, (int64_t)SK)});
+            return RT_OK;
+        }
+        const int64_t kspan = kStridedSpan;
         dim3 g1((unsigned)ceil_div(op.rows, 256), (unsigned)ceil_div(K, kspan));
         emax_strided_kernel<<<g1, 256, 0, stream>>>(op, K, kspan, out.em, err);
         RT_TRY(check_launch("emax_strided_kernel"));
@@ -1441,6 +1503,33 @@ rt_status run(const OzGemm& g, cudaStream_t stream) {
     return finish<S>(P, stream);
 }
 
+// Split-K reductions, then symmetric mirrors, of many products: one grouped
+// launch of each per 48 products.
+template <int S>
+rt_status finish_many(const std::vector<Prepared>& P, cudaStream_t stream) {
+    for (int mirror = 0; mirror < 2; ++mirror) {
+        std::vector<const Prepared*> list;
+        for (const Prepared& x : P)
+            if ((mirror ? x.a.symmetric != 0 : x.a.splits > 1) && x.a.M * x.a.N > 0) list.push_back(&x);
+        for (size_t i0 = 0; i0 < list.size(); i0 += kMaxGroup) {
+            const int cnt = (int)std::min<size_t>(kMaxGroup, list.size() - i0);
+            GroupArgs<kMaxGroup> G;
+            G.n = cnt;
+            G.prefix[0] = 0;
+            for (int i = 0; i < cnt; ++i) {
+                G.a[i] = list[i0 + i]->a;
+                G.prefix[i + 1] = G.prefix[i] + ceil_div(G.a[i].M * G.a[i].N, kFinishBlock);
+            }
+            for (int i = cnt; i < kMaxGroup; ++i) G.prefix[i + 1] = G.prefix[cnt];
+            const unsigned grid = (unsigned)G.prefix[cnt];
+            if (mirror) finish_grouped<S, kMaxGroup, true><<<grid, 256, 0, stream>>>(G);
+            else finish_grouped<S, kMaxGroup, false><<<grid, 256, 0, stream>>>(G);
+            RT_TRY(check_launch("finish_grouped"));
+        }
+    }
+    return RT_OK;
+}
+
 // Many products, grouped into as few launches as possible.
 template <int S>
 rt_status run_many(const OzGemm* gs, int n, cudaStream_t stream) {
@@ -1466,7 +1555,7 @@ rt_status run_many(const OzGemm* gs, int n, cudaStream_t stream) {
             RT_TRY((launch_group<S, kMaxGroup>(grp.data() + i0, cnt, stream)));
         }
     }
-    for (int i = 0; i < n; ++i) RT_TRY(finish<S>(P[i], stream));
+    RT_TRY(finish_many<S>(P, stream));
     return RT_OK;
 }
 
