@@ -232,7 +232,10 @@ rt_status rt_ri_j(const double* B, const double* D, int nb, int naux, double* w,
  * sum_{mu<=nu} (2 - delta_{mu nu}) D[mu,nu] B^P[mu,nu] and J's upper triangle,
  * which it mirrors.  Both passes are bound by the float64 FMA rate, so this
  * takes about half the time of rt_ri_j.  No counterpart in the reference (its
- * ri3fn has the same symmetry; rt_ri_j follows its full contraction). */
+ * ri3fn has the same symmetry; rt_ri_j follows its full contraction).
+ * With RT_CHECK_SYMMETRY=1 in the environment it first compares every mirror
+ * pair of B's first slab and of D, and 64 sampled pairs of every other slab;
+ * a mismatch makes the next rt_sync_status return RT_ERR_INVALID_ARG. */
 rt_status rt_ri_j_symmetric(const double* B, const double* D, int nb, int naux, double* w, double* J, void* stream);
 
 /* Exchange energy E_x = -tr(D K) = -sum_{mu,nu} D[mu,nu] K[mu,nu], reduced in
@@ -420,7 +423,9 @@ rt_status rt_ri_ao2mo_host(const double* C, const double* B, double* ri3mo, int 
  * high-priority stream); pageable B goes by 3-D copies of 32-column blocks.
  * The results are those of rt_ri_ov_k_host on the slabs symmetrised from their
  * upper triangles.  No counterpart in the reference (its ri_ao2mo_f reads the
- * full tensor). */
+ * full tensor).  With RT_CHECK_SYMMETRY=1 in the environment it first compares
+ * every mirror pair of the first slab and 64 sampled pairs of every other slab
+ * in host memory, and returns RT_ERR_INVALID_ARG on a mismatch. */
 rt_status rt_ri_ov_k_host_symmetric(const double* C, const double* B, int nb, int naux, int nocc, int nvir,
                                     double* ov, double* K, int form, int nslices, void* stream);
 

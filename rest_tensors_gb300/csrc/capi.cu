@@ -643,6 +643,10 @@ rt_status rt_ri_j_symmetric(const double* B, const double* D, int nb, int naux, 
         return RT_OK;
     }
     RT_REQUIRE(B && D, "rt_ri_j_symmetric: null input pointer");
+    if (symmetry_check_enabled()) {
+        RT_TRY(symmetry_sample(B, nb, naux, s));
+        RT_TRY(symmetry_sample(D, nb, 1, s));
+    }
     return ri_j_fp64_symmetric(B, D, nb, naux, w, J, s);
 }
 
@@ -1135,6 +1139,8 @@ rt_status rt_ri_ov_k_host(const double* C, const double* B, int nb, int naux, in
 rt_status rt_ri_ov_k_host_symmetric(const double* C, const double* B, int nb, int naux, int nocc, int nvir,
                                     double* ov, double* K, int form, int nslices, void* stream) {
     NvtxRange nvtx_range("rt_ri_ov_k_host_symmetric");
+    if (symmetry_check_enabled() && B && nb > 0)
+        RT_TRY(symmetry_sample_host(B, nb, naux, "rt_ri_ov_k_host_symmetric"));
     return ri_ov_k_host_impl(C, B, nb, naux, nocc, nvir, ov, K, form, nslices, stream, true);
 }
 

@@ -1,10 +1,13 @@
 // rt_common.cu - status text, per-thread error messages, the device error
 // word, and stream-ordered scratch allocation.
 #include <stdarg.h>
+#include <stdlib.h>
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <atomic>
+#include <cmath>
 #include <mutex>
 #include <vector>
 
@@ -60,6 +63,10 @@ rt_status error_word_check(cudaStream_t stream, const char* what) {
     if (h) {
         RT_CUDA_TRY(cudaMemsetAsync(p, 0, sizeof(unsigned int), stream));
         RT_CUDA_TRY(cudaStreamSynchronize(stream));
+        if (h & DEV_ERR_ASYMMETRIC) {
+            set_error(RT_ERR_INVALID_ARG, "%s: an input that must be symmetric is not (sampled check)", what);
+            return RT_ERR_INVALID_ARG;
+        }
         if (h & DEV_ERR_TIMEOUT) {
             set_error(RT_ERR_TIMEOUT, "%s: a device-side wait ran out of its cycle budget", what);
             return RT_ERR_TIMEOUT;
@@ -67,6 +74,76 @@ rt_status error_word_check(cudaStream_t stream, const char* what) {
         set_error(RT_ERR_NONFINITE, "%s: the split form received a non-finite input value", what);
         return RT_ERR_NONFINITE;
     }
+    return RT_OK;
+}
+
+bool symmetry_check_enabled() {
+    static const bool on = [] {
+        const char* v = getenv("RT_CHECK_SYMMETRY");
+        return v && v[0] && v[0] != '0';
+    }();
+    return on;
+}
+
+// Mirror pair t of slab P: a pseudo-random (mu, nu) with mu < nu, the same on
+// host and device.
+__host__ __device__ inline void sample_pair(int nb, int64_t P, int t, int& mu, int& nu) {
+    uint64_t h = (uint64_t)P * 0x9E3779B97F4A7C15ull + (uint64_t)t * 0xBF58476D1CE4E5B9ull + 1;
+    h ^= h >> 31;
+    h *= 0x94D049BB133111EBull;
+    h ^= h >> 29;
+    const int a = (int)(h % (uint64_t)nb), b = (int)((h >> 32) % (uint64_t)nb);
+    mu = a < b ? a : b;
+    nu = a < b ? b : a;
+}
+
+__host__ __device__ inline bool mirror_equal(double x, double y) {
+    const double d = x - y;
+    return fabs(d) <= 1e-12 * (fabs(x) + fabs(y)) || (x == y);
+}
+
+// Every mirror pair of slab 0, then 64 sampled pairs of each slab.
+__global__ void symmetry_sample_kernel(const double* __restrict__ B, int nb, int64_t nslab, unsigned int* err) {
+    const int64_t n2 = (int64_t)nb * nb;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n2; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t mu = e % nb, nu = e / nb;
+        if (mu < nu && !mirror_equal(B[e], B[nu + (int64_t)nb * mu])) atomicOr(err, DEV_ERR_ASYMMETRIC);
+    }
+    for (int64_t P = blockIdx.x; P < nslab; P += gridDim.x) {
+        int mu, nu;
+        sample_pair(nb, P, threadIdx.x, mu, nu);
+        const double* b = B + P * n2;
+        if (!mirror_equal(b[mu + (int64_t)nb * nu], b[nu + (int64_t)nb * mu])) atomicOr(err, DEV_ERR_ASYMMETRIC);
+    }
+}
+
+rt_status symmetry_sample(const double* B, int nb, int64_t nslab, cudaStream_t stream) {
+    if (nb < 2 || nslab <= 0) return RT_OK;
+    unsigned int* err = error_word_device();
+    RT_REQUIRE(err != nullptr, "cannot locate the device error word");
+    symmetry_sample_kernel<<<(unsigned)std::min<int64_t>(nslab, 4 * sm_count()), 64, 0, stream>>>(B, nb, nslab, err);
+    return check_launch("symmetry_sample_kernel");
+}
+
+rt_status symmetry_sample_host(const double* B, int nb, int64_t nslab, const char* what) {
+    const int64_t n2 = (int64_t)nb * nb;
+    for (int nu = 1; nslab > 0 && nu < nb; ++nu)
+        for (int mu = 0; mu < nu; ++mu)
+            if (!mirror_equal(B[mu + (int64_t)nb * nu], B[nu + (int64_t)nb * mu])) {
+                set_error(RT_ERR_INVALID_ARG, "%s: slab 0 is not symmetric at (%d, %d)", what, mu, nu);
+                return RT_ERR_INVALID_ARG;
+            }
+    for (int64_t P = 0; nb >= 2 && P < nslab; ++P)
+        for (int t = 0; t < 64; ++t) {
+            int mu, nu;
+            sample_pair(nb, P, t, mu, nu);
+            const double* b = B + P * n2;
+            if (!mirror_equal(b[mu + (int64_t)nb * nu], b[nu + (int64_t)nb * mu])) {
+                set_error(RT_ERR_INVALID_ARG, "%s: slab %lld is not symmetric at (%d, %d) (sampled check)", what,
+                          (long long)P, mu, nu);
+                return RT_ERR_INVALID_ARG;
+            }
+        }
     return RT_OK;
 }
 

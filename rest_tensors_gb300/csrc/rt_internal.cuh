@@ -80,7 +80,17 @@ unsigned int* error_word_device();
 enum : unsigned int {
     DEV_ERR_NONFINITE = 1u,
     DEV_ERR_TIMEOUT = 2u,
+    DEV_ERR_ASYMMETRIC = 4u,  // a symmetric entry's sampled check found B[mu,nu] != B[nu,mu]
 };
+
+// RT_CHECK_SYMMETRY=1 in the environment (read once per process): the entries
+// whose contract is symmetric slabs sample mirror pairs of their input.
+bool symmetry_check_enabled();
+// Device-side check of nslab [nb, nb] slabs: every mirror pair of the first,
+// 64 sampled pairs of each.
+rt_status symmetry_sample(const double* B, int nb, int64_t nslab, cudaStream_t stream);
+// The same on host memory, synchronously; RT_ERR_INVALID_ARG on a mismatch.
+rt_status symmetry_sample_host(const double* B, int nb, int64_t nslab, const char* what);
 
 int sm_count();
 

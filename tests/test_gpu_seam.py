@@ -100,3 +100,33 @@ def test_seam_runs_the_split_form_when_asked():
     r = subprocess.run([sys.executable, "-c", SPLIT_SEAM], cwd=ROOT, env=env, capture_output=True, text=True,
                        timeout=600)
     assert r.returncode == 0 and "split seam ok" in r.stdout, r.stdout + r.stderr
+
+
+SYMMETRY_CHECK = r"""
+import numpy as np, torch
+import oracle, rest_tensors_gb300 as rt
+nb, naux, nocc = 40, 6, 5
+C, B = oracle.synth_coef(3, nb), oracle.synth_ri3ao(3, nb, naux)
+D = np.asfortranarray(C[:, :nocc] @ C[:, :nocc].T); D = np.asfortranarray(0.5 * (D + D.T))
+Bn = B.copy(order="F"); Bn[7, 30, :] += 1.0  # one mirror pair broken in every slab (slab 0 is checked whole)
+dev = lambda a: torch.from_numpy(np.ascontiguousarray(a.reshape(-1, order="F"))).cuda()
+rt.ri_j(dev(B), dev(D), nb, naux, symmetric=True); rt.sync_status()
+rt.ri_j(dev(Bn), dev(D), nb, naux, symmetric=True)
+try:
+    rt.sync_status(); print("ri_j not refused")
+except rt.RTError as e:
+    assert e.status == 1, e; print("ri_j refused")
+ov = np.zeros((nocc, nb - nocc, naux), order="F"); K = np.zeros((nb, nb), order="F")
+rt.ri_ov_k_host(C, B, nb, naux, nocc, nb - nocc, ov, K, form="fp64", symmetric=True)
+try:
+    rt.ri_ov_k_host(C, Bn, nb, naux, nocc, nb - nocc, ov, K, form="fp64", symmetric=True); print("host not refused")
+except rt.RTError as e:
+    assert e.status == 1, e; print("host refused")
+"""
+
+
+def test_symmetric_entries_check_their_input_when_asked():
+    env = dict(os.environ, RT_CHECK_SYMMETRY="1")
+    r = subprocess.run([sys.executable, "-c", SYMMETRY_CHECK], cwd=ROOT, env=env, capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0 and "ri_j refused" in r.stdout and "host refused" in r.stdout, r.stdout + r.stderr
