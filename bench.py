@@ -70,7 +70,9 @@ def parse():
     p.add_argument("--large-steps", type=int, default=3)
     p.add_argument("--large-full", type=int, default=1,
                    help="also run Davidson on the full 129600-state space of the large system (0: skip)")
-    p.add_argument("--large-full-cycles", type=int, default=300)
+    p.add_argument("--large-full-cycles", type=int, default=1200)
+    p.add_argument("--large-full-residual", type=int, default=4000,
+                   help="also run the full space to residual 1e-8 (tol 1e-16, lindep 1e-24; cycles given here, 0: skip)")
     p.add_argument("--scf", type=int, default=1,
                    help="also time lapack_power and lapack_dspgvx on the device eigensolver (0: skip)")
     p.add_argument("--dropin", type=int, default=1,
@@ -312,6 +314,9 @@ def large_leg(args, rt, torch, stream):
     if args.large_full:
         runs.append(("full_120x1080", nvir, dict(tol=1e-8, maxcyc=args.large_full_cycles, maxspace=100, nroots=8,
                                                  lindep=1e-24), "split"))
+    if args.large_full_residual > 0:
+        runs.append(("full_120x1080_residual_1e-8", nvir, dict(tol=1e-16, maxcyc=args.large_full_residual, maxspace=100,
+                                                               nroots=8, lindep=1e-24), "split"))
     dav = {}
     windows = {}
     for label, nv, prm, mform in runs:
