@@ -310,6 +310,7 @@ __global__ void __launch_bounds__(256) slice_strided_kernel(SliceArgs a) {
 constexpr int kFusedRows = 16;    // contiguous-row slicer
 constexpr int kStridedRows = 16;  // strided-row slicer (8 rows at 3 CTAs/SM measured slower)
 constexpr int kStridedRowsWide = 8;  // 640 < K <= 1280: 8 rows, 32 k-groups of 8 per row
+constexpr int kStridedRowsShort = 32;  // grouped, K <= 320: 32 rows, 8 k-groups of 8 per row
 template <int S, int NBLK, int RR>
 __device__ __forceinline__ void slice_strided_rowmax_body(const SliceArgs& a, int* __restrict__ emax_out,
                                                           int64_t blk) {
@@ -1124,7 +1125,8 @@ rt_status row_exponents(const Operand& op, int64_t K, int* emax, cudaStream_t st
 
 // One-pass slicing jobs collected by the grouped path and launched together.
 struct SliceJob {
-    int kind;   // 0: contiguous rows, 1: strided rows, 2 / 3: row exponents / digits of long strided rows
+    int kind;   // 0: contiguous rows, 1: strided rows (16 per CTA), 2 / 3: row exponents / digits of long
+                // strided rows, 4: short strided rows (32 per CTA)
     int nblk;   // the kernel's NBLK
     SliceArgs sa;
     int* emax;
@@ -1144,6 +1146,17 @@ rt_status launch_slice_group(int kind, int nblk, const SliceGroup& G, unsigned g
     if (kind == 3) {
         slice_strided_grouped<S><<<grid, 256, 0, stream>>>(G);
         return check_launch("slice_strided_grouped");
+    }
+    if (kind == 4) {
+        constexpr int RS = kStridedRowsShort;
+        switch (nblk) {
+            case 1: slice_strided_rowmax_grouped<S, 1, RS><<<grid, 256, 0, stream>>>(G); break;
+            case 2: slice_strided_rowmax_grouped<S, 2, RS><<<grid, 256, 0, stream>>>(G); break;
+            case 3: slice_strided_rowmax_grouped<S, 3, RS><<<grid, 256, 0, stream>>>(G); break;
+            case 4: slice_strided_rowmax_grouped<S, 4, RS><<<grid, 256, 0, stream>>>(G); break;
+            default: slice_strided_rowmax_grouped<S, 5, RS><<<grid, 256, 0, stream>>>(G); break;
+        }
+        return check_launch("slice_strided_rowmax_grouped");
     }
     if (kind == 0) {
         switch (nblk) {
@@ -1253,6 +1266,14 @@ rt_status slice_operand(const Operand& op, int64_t K, int T, Sliced& out, cudaSt
     } else if (op.s0 == 1 && out.Kb * KB <= 640) {
         constexpr int RR = kStridedRows, KQN = 256 / RR;
         const unsigned grid = (unsigned)(out.tiles * T / RR);
+        if (queue && out.Kb * KB <= 320) {
+            // Short rows (small molecules): 32 rows per CTA keep more of its k-slots busy
+            // and give each warp 256-byte runs.
+            constexpr int RS = kStridedRowsShort, KQS = 256 / RS;
+            const int nb = (int)ceil_div(out.Kb * KB, 8 * KQS);
+            queue->jobs.push_back(SliceJob{4, nb, sa, out.em, (int64_t)(out.tiles * T / RS)});
+            return RT_OK;
+        }
         if (queue) {
             const int nb = (int)ceil_div(out.Kb * KB, 8 * KQN);
             queue->jobs.push_back(SliceJob{1, nb <= 4 ? nb : 5, sa, out.em, (int64_t)grid});
