@@ -153,3 +153,22 @@ def test_seam_refuses_an_unknown_form_before_any_device_work(env):
     r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, env={**os.environ, **env}, capture_output=True,
                        text=True, timeout=120)
     assert r.returncode == 0 and "refused" in r.stdout, r.stderr
+
+
+def test_symmetric_host_entry_refuses_asymmetric_input_when_asked():
+    # RT_CHECK_SYMMETRY is read once per process; the host-memory check runs before any device work.
+    import subprocess
+    import sys
+
+    code = ("import numpy as np, rest_tensors_gb300 as rt\n"
+            "nb, naux, nocc = 12, 3, 2\n"
+            "B = np.asfortranarray(np.random.default_rng(0).standard_normal((nb, nb, naux)))\n"
+            "C = np.asfortranarray(np.eye(nb)); ov = np.zeros((nocc, nb - nocc, naux), order='F')\n"
+            "K = np.zeros((nb, nb), order='F')\n"
+            "st = rt.lib().rt_ri_ov_k_host_symmetric(C.ctypes.data, B.ctypes.data, nb, naux, nocc, nb - nocc,\n"
+            "                                         ov.ctypes.data, K.ctypes.data, 0, 7, None)\n"
+            "assert st == 1 and b'not symmetric' in rt.lib().rt_last_error(), (st, rt.lib().rt_last_error())\n"
+            "print('refused')\n")
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, env={**os.environ, "RT_CHECK_SYMMETRY": "1"},
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and "refused" in r.stdout, r.stdout + r.stderr
