@@ -77,10 +77,12 @@ __host__ __device__ constexpr int tmem_cols(int S) { return S * TN <= 256 ? 256 
 // group then has fewer pairs, so an exact chunk is longer.
 __host__ __device__ constexpr bool extra_group(int S) { return (S + 1) * TN <= tmem_cols(S); }
 __host__ __device__ constexpr bool extra_pair(int S, int s) { return extra_group(S) && s >= 1 && (S - s) % 4 == 1; }
-// The first A digit whose lone product goes to the extra group (it starts it).
-__host__ __device__ constexpr int first_extra_pair(int S) {
+// The MMA warp issues A digit s = issue_digit(S, si) at position si: 0, S-1, 1, S-2, ...
+__host__ __device__ constexpr int issue_digit(int S, int si) { return (si & 1) ? S - 1 - (si >> 1) : (si >> 1); }
+// The first A digit, in issue order, whose lone product goes to the extra group.
+__host__ __device__ constexpr int first_issued_extra_pair(int S) {
     int f = -1;
-    for (int s = S - 1; s >= 1; --s) f = extra_pair(S, s) ? s : f;
+    for (int si = S - 1; si >= 0; --si) f = extra_pair(S, issue_digit(S, si)) ? issue_digit(S, si) : f;
     return f;
 }
 // Largest |product| of digits s and t: |d_0| <= 65, |d_s| <= 64 for s >= 1.
@@ -846,15 +848,19 @@ __global__ void __launch_bounds__(FUSED ? NTHREADS_FUSED : NTHREADS, 1)
                         // shared memory and form one K-major operand of 64*(S-s) rows; their
                         // products land in adjacent accumulator groups s .. S-1.  One MMA with
                         // N = 64*(S-s) (split at 256) therefore covers all pairs of digit s.
-                        // A lone product of the last group with s >= 1 goes to the extra group
-                        // (column block S), which the first of them starts on a chunk's first k-step.
+                        // A digits are issued in the order 0, S-1, 1, S-2, ..., which interleaves
+                        // wide and narrow MMAs.  A digit 0 comes first: its MMAs start every
+                        // regular group on a chunk's first k-step.  A lone product of the last
+                        // group with s >= 1 goes to the extra group (column block S), which the
+                        // first of them in issue order starts.
 #pragma unroll
-                        for (int s = 0; s < S; ++s) {
+                        for (int si = 0; si < S; ++si) {
+                            const int s = issue_digit(S, si);
 #pragma unroll
                             for (int t0 = 0; t0 < S - s; t0 += 4) {
                                 const int nt = (S - s - t0) < 4 ? (S - s - t0) : 4;
                                 const bool xg = extra_pair(S, s) && t0 + 1 == S - s;
-                                const uint32_t acc = (first && s == (xg ? first_extra_pair(S) : 0)) ? 0u : 1u;
+                                const uint32_t acc = (first && s == (xg ? first_issued_extra_pair(S) : 0)) ? 0u : 1u;
                                 ptx::mma_bf16_ss(tmem + (uint32_t)((xg ? S : s + t0) * TN),
                                                  adesc0 + soff + (uint64_t)((s * A_BLK) >> 4),
                                                  bdesc0 + soff + (uint64_t)((t0 * B_BLK) >> 4),
