@@ -170,8 +170,8 @@ rt_status rt_ri_ov_k(const double* C, const double* B, int nb, int naux, int noc
  * holds on every GPU that loads it, so nb*nocc may be at most 4,194,304
  * (larger requests fail with RT_ERR_INVALID_ARG); the aux slabs stream through
  * it in blocks.  The first call on each device looks up the array's address
- * (cudaGetSymbolAddress); make that first call before any stream capture.
- * All calls share the array: calls whose kernels overlap on the GPU race. */
+ * (cudaGetSymbolAddress).  All calls share the array: calls whose kernels
+ * overlap on the GPU race. */
 rt_status rt_ri_ov_k_fp64_noalloc(const double* C, const double* B, int nb, int naux, int nocc, int nvir, double* ov,
                                   double* K, void* stream);
 
