@@ -948,8 +948,8 @@ def main():
                 "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": (achieved / peak) if achieved else None,
                 # DRAM bytes per step of the three launches, from an ncu capture of the same
-                # kernels at naux=256 (1.693 GB), scaled by the slab count.
-                "traffic": 1.693e9 * NAUX / 256 if S == 7 else None, "traffic_unit": "bytes per step",
+                # kernels at naux=256 (1.703 GB), scaled by the slab count.
+                "traffic": 1.703e9 * NAUX / 256 if S == 7 else None, "traffic_unit": "bytes per step",
                 "peak_source": f"{pk_kind} bf16_tflops_sustained (kernel timed inside a continuous step loop)",
                 "launches_per_step": g_n / args.steps, "share_of_step": g_ms / (ms * args.steps),
                 "slicing": {"kernel": "emax/slice kernels (HBM)", "achieved_gbs": s_bytes / s_ms / 1e6 if s_ms else None,
