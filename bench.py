@@ -1113,7 +1113,7 @@ def main():
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": workload(), "nbas": NB, "naux": NAUX, "nocc": NOCC, "nvir": NVIR,
                        "form": f"split: {S} BF16 digits per float64, exact FP32 accumulate, int64 recombination",
-                       "nslices": S, "l2": "inputs larger than L2 (6.9 GB ri3ao read per step)",
+                       "nslices": S, "l2": f"inputs larger than L2 ({8e-9 * NB * NB * NAUX:.2f} GB ri3ao read per step)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "fp64": {"value": world * FLOPS / fp64_ms / 1e9, "unit": "TFLOP/s", "ms_per_step": fp64_ms,
                      "form": "float64 DFMA tiled GEMM",
