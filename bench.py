@@ -798,13 +798,13 @@ def run_reference(args, rank: int):
     cores = os.cpu_count() or 1
     oracle.set_threads(cores)
     C = oracle.synth_coef(args.seed, NB)
-    probe = 24
+    probe = max(1, min(24, NAUX))
     B = oracle.synth_ri3ao(args.seed, NB, NAUX, 0, probe)
     oracle.ri_ov_k(C, B, NOCC)
     t0 = time.perf_counter()
     oracle.ri_ov_k(C, B, NOCC)
     per_slab = (time.perf_counter() - t0) / probe
-    nslab = int(max(probe, min(NAUX, per_step_budget / max(per_slab, 1e-9))))
+    nslab = int(max(probe, min(NAUX, per_step_budget / max(per_slab, 1e-9))))  # at most NAUX slabs
     B = oracle.synth_ri3ao(args.seed, NB, NAUX, 0, nslab)
     for _ in range(args.warmup):
         oracle.ri_ov_k(C, B, NOCC)
