@@ -881,9 +881,10 @@ rt_status ri_ov_k_host_impl(const double* C, const double* B, int nb, int naux, 
         if ((e = cudaEventCreateWithFlags(&in[b], cudaEventDisableTiming)) != cudaSuccess) fail(e, "event");
         else if ((e = cudaEventCreateWithFlags(&out[b], cudaEventDisableTiming)) != cudaSuccess) fail(e, "event");
     }
+    if (st == RT_OK && (e = cudaMemcpyAsync(dC.p, C, sizeof(double) * nC, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        fail(e, "host-to-device copy");
     if (st == RT_OK) {
         // The pool allocations above are ordered on `s`; the copy streams start after them.
-        cudaMemcpyAsync(dC.p, C, sizeof(double) * nC, cudaMemcpyHostToDevice, s);
         cudaEventRecord(ready, s);
         cudaStreamWaitEvent(hs, ready, 0);
         cudaStreamWaitEvent(ds, ready, 0);
